@@ -1,0 +1,163 @@
+"""
+Chain contractions with the signatures of pytenet/chain_ops.py, computed by the
+GPU kernels. Inputs may be NumPy arrays (results are returned as NumPy arrays,
+like the reference) or complex128 CUDA tensors (results stay on the device).
+"""
+
+import numpy as np
+import torch
+
+from . import _lib
+from .device import Workspace, call, empty, lib, ptr, stream_ptr, to_dev, to_host
+
+__all__ = ["apply_local_hamiltonian", "apply_local_bond_contraction",
+           "contraction_operator_step_left", "contraction_operator_step_right",
+           "compute_right_operator_blocks", "mpo_average", "mpo_inner_product",
+           "mps_vdot", "mps_norm"]
+
+_WS = Workspace()
+
+
+def _is_host(*xs):
+    return not any(isinstance(x, torch.Tensor) for x in xs)
+
+
+def _ret(t, host):
+    return to_host(t) if host else t
+
+
+def apply_local_hamiltonian(a, w, l, r, precision="fp64"):
+    """H_eff . a (pytenet/chain_ops.py:237-279): out[l2, s, r2]."""
+    from .engine import prec_code
+    assert a.ndim == 3 and w.ndim == 4 and l.ndim == 3 and r.ndim == 3
+    host = _is_host(a, w, l, r)
+    Dl, d, Dr = a.shape
+    cl, cr = w.shape[0], w.shape[3]
+    assert tuple(l.shape) == (Dl, cl, Dl) and tuple(r.shape) == (Dr, cr, Dr)
+    assert w.shape[1] == d and w.shape[2] == d
+    A, W, Lt, R = (to_dev(x) for x in (a, w, l, r))
+    out = empty((Dl, d, Dr))
+    p = prec_code(precision)
+    L = lib()
+    wsb = L.ptn_heff_workspace_bytes(Dl, d, Dr, cl, cr, p)
+    call(L.ptn_heff_apply, ptr(A), ptr(W), ptr(Lt), ptr(R), ptr(out), Dl, d, Dr, cl, cr, p,
+         ptr(_WS.get(wsb)), wsb, stream_ptr())
+    return _ret(out, host)
+
+
+def apply_local_bond_contraction(c, l, r, precision="fp64"):
+    """Zero-site H_eff . c (pytenet/chain_ops.py:282-317): out[l2, r2]."""
+    from .engine import prec_code
+    assert c.ndim == 2 and l.ndim == 3 and r.ndim == 3
+    host = _is_host(c, l, r)
+    Dl, Dr = c.shape
+    chi = l.shape[1]
+    assert tuple(l.shape) == (Dl, chi, Dl) and tuple(r.shape) == (Dr, chi, Dr)
+    Cm, Lt, R = (to_dev(x) for x in (c, l, r))
+    out = empty((Dl, Dr))
+    p = prec_code(precision)
+    L = lib()
+    wsb = L.ptn_bond_workspace_bytes(Dl, Dr, chi, p)
+    call(L.ptn_bond_apply, ptr(Cm), ptr(Lt), ptr(R), ptr(out), Dl, Dr, chi, p, ptr(_WS.get(wsb)),
+         wsb, stream_ptr())
+    return _ret(out, host)
+
+
+def contraction_operator_step_left(a, b, w, l):
+    """Left environment step (pytenet/chain_ops.py:60-99): l_next[r_a, chi_r, r_b]."""
+    assert a.ndim == 3 and b.ndim == 3 and w.ndim == 4 and l.ndim == 3
+    assert tuple(a.shape) == tuple(b.shape), "a and b must have equal shapes"
+    host = _is_host(a, b, w, l)
+    Dl, d, Dr = a.shape
+    cl, cr = w.shape[0], w.shape[3]
+    assert tuple(l.shape) == (Dl, cl, Dl)
+    A, B, W, Lt = (to_dev(x) for x in (a, b, w, l))
+    out = empty((Dr, cr, Dr))
+    L = lib()
+    wsb = L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, 0)
+    call(L.ptn_env_step_left, ptr(A), ptr(B), ptr(W), ptr(Lt), ptr(out), Dl, d, Dr, cl, cr, 0,
+         ptr(_WS.get(wsb)), wsb, stream_ptr())
+    return _ret(out, host)
+
+
+def contraction_operator_step_right(a, b, w, r):
+    """Right environment step (pytenet/chain_ops.py:16-57): r_next[l_a, chi_l, l_b]."""
+    assert a.ndim == 3 and b.ndim == 3 and w.ndim == 4 and r.ndim == 3
+    assert tuple(a.shape) == tuple(b.shape), "a and b must have equal shapes"
+    host = _is_host(a, b, w, r)
+    Dl, d, Dr = a.shape
+    cl, cr = w.shape[0], w.shape[3]
+    assert tuple(r.shape) == (Dr, cr, Dr)
+    A, B, W, R = (to_dev(x) for x in (a, b, w, r))
+    out = empty((Dl, cl, Dl))
+    L = lib()
+    wsb = L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, 0)
+    call(L.ptn_env_step_right, ptr(A), ptr(B), ptr(W), ptr(R), ptr(out), Dl, d, Dr, cl, cr, 0,
+         ptr(_WS.get(wsb)), wsb, stream_ptr())
+    return _ret(out, host)
+
+
+def compute_right_operator_blocks(psi, op):
+    """All right environments (pytenet/chain_ops.py:102-113), as device tensors."""
+    n = psi.nsites
+    assert n == op.nsites
+    blocks = [None] * n
+    blocks[n - 1] = to_dev(np.array([[[1.0]]]))
+    for i in reversed(range(n - 1)):
+        blocks[i] = contraction_operator_step_right(to_dev(psi.a[i + 1]), to_dev(psi.a[i + 1]),
+                                                    to_dev(op.a[i + 1]), blocks[i + 1])
+    return blocks
+
+
+def mpo_inner_product(chi, op, psi):
+    """<chi|op|psi> (pytenet/chain_ops.py:165-189); chi and psi must share their
+    bond dimensions (the square-environment kernels)."""
+    assert chi.nsites == op.nsites and psi.nsites == op.nsites
+    if psi.nsites == 0:
+        return 0
+    n = psi.a[-1].shape[2]
+    t = to_dev(np.identity(n).reshape((n, 1, n)))
+    for i in reversed(range(psi.nsites)):
+        t = contraction_operator_step_right(to_dev(psi.a[i]), to_dev(chi.a[i]), to_dev(op.a[i]), t)
+    assert tuple(t.shape) == (1, 1, 1)
+    return complex(t.reshape(-1)[0].item())
+
+
+def mpo_average(psi, op):
+    """<psi|op|psi> (pytenet/chain_ops.py:151-162)."""
+    return mpo_inner_product(psi, op, psi)
+
+
+def _zgemm(opa, opb, M, N, K, A, lda, B, ldb, Cout, ldc):
+    L = lib()
+    wsb = L.ptn_zgemm_workspace_bytes(M, N, K, 1)
+    call(L.ptn_zgemm, opa, opb, M, N, K, _lib.cval(1), ptr(A), lda, 0, ptr(B), ldb, 0,
+         _lib.cval(0), ptr(Cout), ldc, 0, 1, ptr(_WS.get(wsb)), wsb, stream_ptr())
+
+
+def mps_vdot(chi, psi):
+    """<chi|psi> (pytenet/mps.py:430-450), contracted from the right on the GPU."""
+    assert chi.nsites == psi.nsites
+    if psi.nsites == 0:
+        return 0
+    n = psi.a[-1].shape[2]
+    t = to_dev(np.identity(n))               # (Dpsi_r, Dchi_r)
+    for i in reversed(range(psi.nsites)):
+        a = to_dev(psi.a[i])
+        b = to_dev(chi.a[i])
+        Dl, d, Dr = a.shape
+        El, _, Er = b.shape
+        # u[(l, s), e] = sum_r a[(l, s), r] t[r, e]
+        u = empty((Dl, d, Er))
+        _zgemm(b"N", b"N", Dl * d, Er, Dr, a, Dr, t, Er, u, Er)
+        # t'[l, f] = sum_(s, e) u[l, (s, e)] conj(b[f, (s, e)])
+        tn = empty((Dl, El))
+        _zgemm(b"N", b"H", Dl, El, d * Er, u, d * Er, b, d * Er, tn, El)
+        t = tn
+    assert tuple(t.shape) == (1, 1)
+    return complex(t.reshape(-1)[0].item())
+
+
+def mps_norm(psi):
+    """(pytenet/mps.py:453-457)"""
+    return float(np.sqrt(mps_vdot(psi, psi).real))

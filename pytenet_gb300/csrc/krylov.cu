@@ -1,0 +1,460 @@
+// Krylov core of the sweep (pytenet/krylov.py:12-150), fully on the device.
+//
+// lanczos_iteration (krylov.py:12-57) is split into memory-bound passes over the
+// n-vectors; every reduction is two-phase (per-CTA partials, then each consumer
+// CTA re-reduces the partials in a fixed order), so results are deterministic and
+// no pass needs a host round trip:
+//   start : nrm = |v|, V[0] = v / nrm
+//   step j: (w = A V[j] already in V[j+1])
+//           alpha_j = Re <w, V[j]>                            dot pass
+//           w -= alpha_j V[j] + beta_{j-1} V[j-1]; |w|^2        update pass
+//           beta_j = |w|; breakdown if beta_j < 100 n eps, else V[j+1] = w / beta_j
+//   last  : alpha_{m-1} = Re <A V[m-1], V[m-1]> and the residual norm beta_next
+// A breakdown sets state->stopped: all later passes (and the operator launches,
+// which test the same flag) return immediately, m_used keeps the truncated size,
+// exactly the early return of krylov.py:44-50.
+// The tridiagonal eigenproblem (eigh_tridiag, krylov.py:142-150) is solved by one
+// warp with the implicit QL algorithm with Wilkinson shifts (Bowdler, Martin,
+// Reinsch, Wilkinson 1968); lane k carries row k of the eigenvector matrix, every
+// lane runs the same scalar recurrence, so no synchronisation is needed.
+// expm_krylov (krylov.py:122-136) and eigh_krylov (krylov.py:110-119) then reduce
+// to coefficients c_k and one combination pass out = sum_k c_k V[k].
+#include "ptn_common.cuh"
+#include <cfloat>
+#include <algorithm>
+
+namespace ptn {
+
+void note_launches(int n);
+
+namespace {
+
+constexpr int RED_MAX = 1024;   // max CTAs of a vector pass (partials per reduction)
+constexpr int VT = 256;         // threads per CTA of a vector pass
+
+struct KState {
+  ptn_krylov_state s;
+  double part_a[RED_MAX];
+  double part_b[RED_MAX];
+  int nblocks;                  // CTAs used by the vector passes of this run
+};
+
+__device__ __forceinline__ double reduce_partials(const double* part, int nb, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v += part[i];
+  return block_sum(v, sh);
+}
+
+__global__ void __launch_bounds__(VT) k_norm_partial(KState* st, const double2* __restrict__ x,
+                                                     long n) {
+  __shared__ double sh[33];
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)VT + threadIdx.x; i < n; i += (long)gridDim.x * VT) {
+    const double2 v = x[i];
+    acc = fma(v.x, v.x, acc);
+    acc = fma(v.y, v.y, acc);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) st->part_a[blockIdx.x] = acc;
+}
+
+__global__ void __launch_bounds__(VT) k_start_finish(KState* st, const double2* __restrict__ x,
+                                                     double2* __restrict__ v0, long n, int maxiter) {
+  __shared__ double sh[33];
+  const int nb = gridDim.x;
+  const double nrm = sqrt(reduce_partials(st->part_a, nb, sh));
+  const bool ok = (nrm > 0.0) && isfinite(nrm);
+  if (ok) {
+    const double inv = 1.0 / nrm;
+    for (long i = blockIdx.x * (long)VT + threadIdx.x; i < n; i += (long)gridDim.x * VT) {
+      const double2 v = x[i];
+      v0[i] = make_double2(v.x * inv, v.y * inv);
+    }
+  }
+  if (blockIdx.x == 0) {
+    for (int i = threadIdx.x; i < PTN_KRYLOV_MAXITER; i += blockDim.x) {
+      st->s.alpha[i] = 0.0;
+      st->s.beta[i] = 0.0;
+      st->s.coef[i].re = 0.0;
+      st->s.coef[i].im = 0.0;
+    }
+    if (threadIdx.x == 0) {
+      st->s.nrm = nrm;
+      st->s.m_used = 1;
+      st->s.stopped = ok ? 0 : 1;
+      st->s.maxiter = maxiter;
+      st->s.status = ok ? PTN_OK : PTN_NAN;
+      st->s.beta_next = 0.0;
+      st->s.eval0 = 0.0;
+      st->s.resid = 0.0;
+      st->nblocks = nb;
+    }
+  }
+}
+
+// partial Re <w, v> = sum w.x v.x + w.y v.y
+__global__ void __launch_bounds__(VT) k_dot_partial(KState* st, const double2* __restrict__ w,
+                                                    const double2* __restrict__ v, long n) {
+  if (st->s.stopped) return;
+  __shared__ double sh[33];
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)VT + threadIdx.x; i < n; i += (long)gridDim.x * VT) {
+    const double2 a = w[i], b = v[i];
+    acc = fma(a.x, b.x, acc);
+    acc = fma(a.y, b.y, acc);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) st->part_a[blockIdx.x] = acc;
+}
+
+// w -= alpha_j v_j + beta_{j-1} v_{j-1}; partial |w|^2. With `inplace` false the
+// residual norm is accumulated without writing w (final iteration).
+__global__ void __launch_bounds__(VT) k_update(KState* st, double2* __restrict__ w,
+                                               const double2* __restrict__ vj,
+                                               const double2* __restrict__ vjm1, long n, int j,
+                                               int inplace) {
+  if (st->s.stopped) return;
+  __shared__ double sh[33];
+  const double alpha = reduce_partials(st->part_a, gridDim.x, sh);
+  const double beta = (j > 0) ? st->s.beta[j - 1] : 0.0;
+  double acc = 0.0;
+  for (long i = blockIdx.x * (long)VT + threadIdx.x; i < n; i += (long)gridDim.x * VT) {
+    const double2 a = vj[i];
+    double2 t = make_double2(alpha * a.x, alpha * a.y);
+    if (j > 0) {
+      const double2 b = vjm1[i];
+      t.x += beta * b.x;
+      t.y += beta * b.y;
+    }
+    double2 x = w[i];
+    x.x -= t.x;
+    x.y -= t.y;
+    if (inplace) w[i] = x;
+    acc = fma(x.x, x.x, acc);
+    acc = fma(x.y, x.y, acc);
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) {
+    st->part_b[blockIdx.x] = acc;
+    if (blockIdx.x == 0) st->s.alpha[j] = alpha;
+  }
+}
+
+__global__ void __launch_bounds__(VT) k_scale(KState* st, double2* __restrict__ w, long n, int j,
+                                              double thresh) {
+  if (st->s.stopped) return;
+  __shared__ double sh[33];
+  const double beta = sqrt(reduce_partials(st->part_b, gridDim.x, sh));
+  if (beta < thresh) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->s.beta_next = beta;
+      st->s.m_used = j + 1;
+      st->s.stopped = 1;
+      st->s.breakdowns += 1;
+    }
+    return;
+  }
+  const double inv = 1.0 / beta;
+  for (long i = blockIdx.x * (long)VT + threadIdx.x; i < n; i += (long)gridDim.x * VT) {
+    double2 x = w[i];
+    w[i] = make_double2(x.x * inv, x.y * inv);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->s.beta[j] = beta;
+    st->s.m_used = j + 2;
+  }
+}
+
+// final alpha; beta_next comes from the partials of a non-writing update pass
+__global__ void k_last_alpha(KState* st, int j) {
+  if (st->s.stopped) return;
+  __shared__ double sh[33];
+  const double alpha = reduce_partials(st->part_a, st->nblocks, sh);
+  if (threadIdx.x == 0) st->s.alpha[j] = alpha;
+}
+
+__global__ void k_last_resid(KState* st) {
+  if (st->s.stopped) return;
+  __shared__ double sh[33];
+  const double b = sqrt(reduce_partials(st->part_b, st->nblocks, sh));
+  if (threadIdx.x == 0) st->s.beta_next = b;
+}
+
+// Symmetric tridiagonal eigenproblem by implicit QL with Wilkinson shifts.
+// d[0..n-1] diagonal, e[0..n-2] off-diagonal (e[n-1] ignored); on return d holds
+// the eigenvalues and z (this lane's row of the eigenvector matrix) the rotations.
+__device__ void tridiag_ql(double* d, double* e, int n, double* z) {
+  if (n > 0) e[n - 1] = 0.0;
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0; iter < 80; ++iter) {
+      int mm = l;
+      for (; mm < n - 1; ++mm) {
+        const double dd = fabs(d[mm]) + fabs(d[mm + 1]);
+        if (fabs(e[mm]) <= DBL_EPSILON * dd) break;
+      }
+      if (mm == l) break;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = hypot(g, 1.0);
+      g = d[mm] - d[l] + e[l] / (g + copysign(r, g));
+      double s = 1.0, c = 1.0, p = 0.0;
+      bool deflated = false;
+      for (int i = mm - 1; i >= l; --i) {
+        const double f = s * e[i], b = c * e[i];
+        r = hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] -= p;
+          e[mm] = 0.0;
+          deflated = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * s + 2.0 * c * b;
+        p = s * r;
+        d[i + 1] = g + p;
+        g = c * r - b;
+        const double zi = z[i], zi1 = z[i + 1];
+        z[i + 1] = s * zi + c * zi1;
+        z[i] = c * zi - s * zi1;
+      }
+      if (deflated) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[mm] = 0.0;
+    }
+  }
+}
+
+// mode 0: expm coefficients c = nrm U exp(dt Lambda) U^T e_1;
+// mode 1: lowest Ritz vector coefficients c = U[:, argmin], eval0 = min eigenvalue.
+__global__ void k_tridiag(KState* st, double dt_re, double dt_im, int mode) {
+  const int lane = threadIdx.x;  // one warp
+  if (st->s.status != PTN_OK) return;
+  const int m = st->s.m_used;
+  double d[PTN_KRYLOV_MAXITER], e[PTN_KRYLOV_MAXITER], z[PTN_KRYLOV_MAXITER];
+  for (int i = 0; i < m; ++i) {
+    d[i] = st->s.alpha[i];
+    e[i] = (i < m - 1) ? st->s.beta[i] : 0.0;
+  }
+  // lanes >= 32 never exist; rows k >= 32 are handled by a second pass below
+  for (int pass = 0; pass * 32 < m; ++pass) {
+    const int k = pass * 32 + lane;
+    double dd[PTN_KRYLOV_MAXITER], ee[PTN_KRYLOV_MAXITER];
+    for (int i = 0; i < m; ++i) { dd[i] = d[i]; ee[i] = e[i]; z[i] = (i == k) ? 1.0 : 0.0; }
+    tridiag_ql(dd, ee, m, z);
+    // row 0 of U (lane 0 of pass 0 owns it): broadcast through shared memory
+    __shared__ double u0[PTN_KRYLOV_MAXITER];
+    __shared__ double lam[PTN_KRYLOV_MAXITER];
+    if (pass == 0 && lane == 0)
+      for (int i = 0; i < m; ++i) { u0[i] = z[i]; lam[i] = dd[i]; }
+    __syncwarp();
+    if (k < m) {
+      if (mode == 0) {
+        double cr = 0.0, ci = 0.0;
+        for (int jj = 0; jj < m; ++jj) {
+          const double a = exp(dt_re * lam[jj]);
+          double sn, cs;
+          sincos(dt_im * lam[jj], &sn, &cs);
+          const double f = st->s.nrm * u0[jj] * z[jj];
+          cr = fma(f * a, cs, cr);
+          ci = fma(f * a, sn, ci);
+        }
+        st->s.coef[k].re = cr;
+        st->s.coef[k].im = ci;
+      } else {
+        int jmin = 0;
+        for (int jj = 1; jj < m; ++jj)
+          if (lam[jj] < lam[jmin]) jmin = jj;
+        st->s.coef[k].re = z[jmin];
+        st->s.coef[k].im = 0.0;
+        if (k == 0) st->s.eval0 = lam[jmin];
+      }
+    }
+    __syncwarp();
+  }
+  __syncwarp();
+  if (lane == 0) {
+    const ptn_c128 cl = st->s.coef[m - 1];
+    st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im);
+  }
+}
+
+// Full eigen-decomposition of the tridiagonal matrix, eigenvalues ascending as
+// numpy.linalg.eigh returns them: evals[j], evecs[k * m + j] = U[k][j].
+__global__ void k_tridiag_eig(const KState* st, double* evals, double* evecs) {
+  const int lane = threadIdx.x;
+  if (st->s.status != PTN_OK) return;
+  const int m = st->s.m_used;
+  __shared__ int perm[PTN_KRYLOV_MAXITER];
+  double d[PTN_KRYLOV_MAXITER], e[PTN_KRYLOV_MAXITER], z[PTN_KRYLOV_MAXITER];
+  for (int pass = 0; pass * 32 < m; ++pass) {
+    const int k = pass * 32 + lane;
+    for (int i = 0; i < m; ++i) {
+      d[i] = st->s.alpha[i];
+      e[i] = (i < m - 1) ? st->s.beta[i] : 0.0;
+      z[i] = (i == k) ? 1.0 : 0.0;
+    }
+    tridiag_ql(d, e, m, z);
+    if (pass == 0 && lane == 0) {
+      for (int i = 0; i < m; ++i) perm[i] = i;
+      for (int i = 1; i < m; ++i) {           // insertion sort, stable
+        const int p = perm[i];
+        int j = i - 1;
+        while (j >= 0 && d[perm[j]] > d[p]) { perm[j + 1] = perm[j]; --j; }
+        perm[j + 1] = p;
+      }
+      for (int i = 0; i < m; ++i) evals[i] = d[perm[i]];
+    }
+    __syncwarp();
+    if (k < m)
+      for (int j = 0; j < m; ++j) evecs[(long)k * m + j] = z[perm[j]];
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(VT) k_combine(const KState* st, const double2* __restrict__ V,
+                                                long n, double2* __restrict__ out) {
+  if (st->s.status != PTN_OK) return;
+  const int m = st->s.m_used;
+  for (long i = blockIdx.x * (long)VT + threadIdx.x; i < n; i += (long)gridDim.x * VT) {
+    double2 acc = make_double2(0.0, 0.0);
+    for (int k = 0; k < m; ++k) {
+      const ptn_c128 c = st->s.coef[k];
+      acc = cfma(make_double2(c.re, c.im), V[(long)k * n + i], acc);
+    }
+    out[i] = acc;
+  }
+}
+
+int vec_blocks(long n) {
+  long b = (n + 4L * VT - 1) / (4L * VT);
+  b = std::max(1L, std::min(b, (long)std::min(RED_MAX, 8 * num_sms())));
+  return (int)b;
+}
+
+}  // namespace
+
+size_t krylov_state_bytes() { return (sizeof(KState) + 255) & ~size_t(255); }
+const int32_t* krylov_stop_flag(const void* state) {
+  return &static_cast<const KState*>(state)->s.stopped;
+}
+
+ptn_status krylov_start(void* state, const double2* vstart, double2* V, long n, int maxiter,
+                        cudaStream_t st) {
+  PTN_CHECK_ARG(n > 0, "krylov: empty vector");
+  PTN_CHECK_ARG(maxiter >= 1 && maxiter <= PTN_KRYLOV_MAXITER,
+                "krylov: numiter must be in [1, %d]", PTN_KRYLOV_MAXITER);
+  KState* s = static_cast<KState*>(state);
+  const int nb = vec_blocks(n);
+  k_norm_partial<<<nb, VT, 0, st>>>(s, vstart, n);
+  k_start_finish<<<nb, VT, 0, st>>>(s, vstart, V, n, maxiter);
+  PTN_LAUNCH_CHECK();
+  note_launches(2);
+  return PTN_OK;
+}
+
+ptn_status krylov_step(void* state, double2* V, long n, int j, cudaStream_t st) {
+  KState* s = static_cast<KState*>(state);
+  const int nb = vec_blocks(n);
+  const double thresh = 100.0 * (double)n * DBL_EPSILON;
+  double2* w = V + (long)(j + 1) * n;
+  const double2* vj = V + (long)j * n;
+  const double2* vjm1 = j > 0 ? V + (long)(j - 1) * n : vj;
+  k_dot_partial<<<nb, VT, 0, st>>>(s, w, vj, n);
+  k_update<<<nb, VT, 0, st>>>(s, w, vj, vjm1, n, j, 1);
+  k_scale<<<nb, VT, 0, st>>>(s, w, n, j, thresh);
+  PTN_LAUNCH_CHECK();
+  note_launches(3);
+  return PTN_OK;
+}
+
+ptn_status krylov_last(void* state, const double2* V, const double2* w, long n, int j, bool resid,
+                       cudaStream_t st) {
+  KState* s = static_cast<KState*>(state);
+  const int nb = vec_blocks(n);
+  const double2* vj = V + (long)j * n;
+  const double2* vjm1 = j > 0 ? V + (long)(j - 1) * n : vj;
+  k_dot_partial<<<nb, VT, 0, st>>>(s, w, vj, n);
+  int launches = 1;
+  if (resid) {
+    k_update<<<nb, VT, 0, st>>>(s, const_cast<double2*>(w), vj, vjm1, n, j, 0);
+    k_last_resid<<<1, 256, 0, st>>>(s);
+    launches += 2;
+  } else {
+    k_last_alpha<<<1, 256, 0, st>>>(s, j);
+    launches += 1;
+  }
+  PTN_LAUNCH_CHECK();
+  note_launches(launches);
+  return PTN_OK;
+}
+
+ptn_status krylov_coef(void* state, double dt_re, double dt_im, int mode, cudaStream_t st) {
+  k_tridiag<<<1, 32, 0, st>>>(static_cast<KState*>(state), dt_re, dt_im, mode);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
+}
+
+ptn_status krylov_tridiag_eig(const void* state, double* evals, double* evecs, cudaStream_t st) {
+  k_tridiag_eig<<<1, 32, 0, st>>>(static_cast<const KState*>(state), evals, evecs);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
+}
+
+ptn_status krylov_combine(const void* state, const double2* V, long n, double2* out,
+                          cudaStream_t st) {
+  k_combine<<<vec_blocks(n), VT, 0, st>>>(static_cast<const KState*>(state), V, n, out);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
+}
+
+}  // namespace ptn
+
+using namespace ptn;
+
+extern "C" {
+
+size_t ptn_krylov_state_bytes(void) { return krylov_state_bytes(); }
+const int32_t* ptn_krylov_stop_flag(const void* state) { return krylov_stop_flag(state); }
+
+ptn_status ptn_krylov_start(void* state, const ptn_c128* vstart, ptn_c128* V, long n, int maxiter,
+                            void* stream) {
+  return krylov_start(state, reinterpret_cast<const double2*>(vstart),
+                      reinterpret_cast<double2*>(V), n, maxiter, as_stream(stream));
+}
+
+ptn_status ptn_krylov_step(void* state, ptn_c128* V, long n, int j, void* stream) {
+  return krylov_step(state, reinterpret_cast<double2*>(V), n, j, as_stream(stream));
+}
+
+ptn_status ptn_krylov_last(void* state, const ptn_c128* V, const ptn_c128* w, long n, int j,
+                           void* stream) {
+  // the generic path always reports the residual norm (one extra vector pass)
+  return krylov_last(state, reinterpret_cast<const double2*>(V),
+                     reinterpret_cast<const double2*>(w), n, j, true, as_stream(stream));
+}
+
+ptn_status ptn_krylov_expm_coef(void* state, double dt_re, double dt_im, void* stream) {
+  return krylov_coef(state, dt_re, dt_im, 0, as_stream(stream));
+}
+
+ptn_status ptn_krylov_eigh_coef(void* state, void* stream) {
+  return krylov_coef(state, 0.0, 0.0, 1, as_stream(stream));
+}
+
+ptn_status ptn_krylov_tridiag_eig(const void* state, double* evals, double* evecs, void* stream) {
+  return krylov_tridiag_eig(state, evals, evecs, as_stream(stream));
+}
+
+ptn_status ptn_krylov_combine(const void* state, const ptn_c128* V, long n, ptn_c128* out,
+                              void* stream) {
+  return krylov_combine(state, reinterpret_cast<const double2*>(V), n,
+                        reinterpret_cast<double2*>(out), as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,121 @@
+"""Host-side logic of pytenet_gb300 (no GPU): the C ABI library loads and exports
+every declared symbol, integer quantum-number plans match the reference, the
+input generators reproduce the reference's draws and operators."""
+
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, load_golden, golden_mps, golden_mpo
+from oracle import ptn_oracle as orc
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "pytenet_gb300.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(ptn_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol():
+    import ctypes
+    from pytenet_gb300 import build
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    syms = header_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+    from pytenet_gb300 import _lib
+    assert set(_lib.exported_names()) == set(syms)
+    L = _lib.load(path)
+    assert L.ptn_abi_version() == 1
+    assert b"sm_103a" in L.ptn_version()
+
+
+def test_workspace_queries_need_no_gpu():
+    from pytenet_gb300 import _lib
+    L = _lib.load()
+    assert L.ptn_krylov_state_bytes() >= ctypes_sizeof_state()
+    assert L.ptn_qr_workspace_bytes(1024, 512) > 1024 * 512 * 16
+    assert L.ptn_heff_workspace_bytes(64, 2, 64, 5, 5, 0) >= 2 * 64 * 10 * 64 * 16
+
+
+def ctypes_sizeof_state():
+    import ctypes
+    from pytenet_gb300 import _lib
+    return ctypes.sizeof(_lib.KrylovState)
+
+
+def test_qr_plans_match_reference_bookkeeping():
+    from pytenet_gb300.qnumber import qr_plan
+    g = load_golden("block_qr.npz")
+    for k in range(int(g["ncases"])):
+        plan = qr_plan(g[f"q0_{k}"], g[f"q1_{k}"])
+        assert np.array_equal(plan.qinterm, g[f"qi{k}"])
+        assert plan.K == g[f"q{k}"].shape[1]
+
+
+def test_random_mps_draw_order():
+    import pytenet_gb300 as ptg
+    g = load_golden("mps_random.npz")
+    ref = golden_mps(g, "r_")
+    psi = ptg.MPS(ref.qsite, ref.qbonds, fill="random", rng=np.random.default_rng(1009))
+    for x, y in zip(psi.a, ref.a):
+        assert np.array_equal(x, y)
+    ref = golden_mps(g, "c_")
+    psi = ptg.MPS.construct_random(7, [1, -1], 1, max_vdim=6, dtype="complex",
+                                   rng=np.random.default_rng(1010))
+    for q, qr in zip(psi.qbonds, ref.qbonds):
+        assert np.array_equal(q, qr)
+    for x, y in zip(psi.a, ref.a):
+        assert np.array_equal(x, y)
+    ref = golden_mps(g, "d_")
+    psi = ptg.MPS.construct_random(6, [1, -1], 0, max_vdim=5, dtype="real",
+                                   rng=np.random.default_rng(1011))
+    for x, y in zip(psi.a, ref.a):
+        assert np.array_equal(x, y)
+
+
+@pytest.mark.parametrize("L", [2, 3, 4, 5, 6])
+def test_hamiltonians_equal_reference_operators(L):
+    import pytenet_gb300 as ptg
+    g = load_golden("mpos.npz")
+    h = ptg.heisenberg_xxz_1d_mpo(L, 1.3, 0.7, -0.2)
+    assert np.allclose(h.to_matrix(), g[f"xxz{L}_mat"], rtol=0, atol=1e-14)
+    assert np.allclose(orc.mpo_to_matrix(h), g[f"xxz{L}_mat"], rtol=0, atol=1e-14)
+    for i, w in enumerate(h.a):
+        assert orc.is_qsparse(w, (h.qbonds[i], h.qsite, -h.qsite, -h.qbonds[i + 1]))
+    s = ptg.ising_1d_mpo(L, 1.0, 0.15, 0.8)
+    assert np.allclose(s.to_matrix(), g[f"ising{L}_mat"], rtol=0, atol=1e-14)
+
+
+def test_to_vector_matches_oracle():
+    import pytenet_gb300 as ptg
+    g = load_golden("tdvp_readme.npz")
+    ref = golden_mps(g, "p1_")
+    psi = ptg.MPS(ref.qsite, ref.qbonds, fill="postpone")
+    psi.a = [x.copy() for x in ref.a]
+    assert np.allclose(psi.to_vector(), g["v1"], atol=1e-14)
+    assert np.allclose(psi.as_vector(), orc.mps_to_vector(ref), atol=1e-14)
+
+
+def test_product_package_does_not_import_oracle():
+    pkg = os.path.join(ROOT, "pytenet_gb300")
+    for f in os.listdir(pkg):
+        if f.endswith(".py"):
+            src = open(os.path.join(pkg, f)).read()
+            assert "oracle" not in src.replace("the oracle", ""), f
+
+
+def test_no_gpu_means_loud_failure():
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    import pytenet_gb300 as ptg
+    h = ptg.heisenberg_xxz_1d_mpo(4, 1.0, 0.8, -0.1)
+    psi = ptg.MPS(h.qsite, [[0], [0, 0], [0, 0], [0, 0], [0]], fill="random",
+                  rng=np.random.default_rng(0))
+    with pytest.raises(RuntimeError):
+        ptg.tdvp_singlesite(h, psi, 0.1j, 1, numiter_lanczos=3)
