@@ -1,0 +1,380 @@
+"""
+Benchmark: single-site TDVP site-updates/s on the XXZ chain, L=64, D=512
+(dt = 0.05j, numiter_lanczos = 10, Delta drawn uniformly in [0.5, 1.5] from a
+seeded generator, zero quantum numbers, seeded complex Gaussian left-orthonormal
+MPS with bonds min(2^min(i, L-i), D)).
+
+One "step" is one symmetric TDVP time step = 2L-1 site updates. Inputs are
+resident in HBM when the timed region starts; the whole state (site tensors,
+environments, Krylov basis: several GB) is far larger than the 129 MB L2, so no
+explicit L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|fp64]
+  python bench.py --impl reference ...   # the reference CPU algorithm (NumPy oracle
+                                         # port) on this host's cores, same metric
+
+Multi-GPU: the sweep does not shard (site i+1 depends on site i), so N GPUs run
+N independent replicas of the workload (weak scaling, no collective on the data
+path); value = total site updates / max-over-ranks time.
+"""
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TDVP site-updates/s, XXZ L=64 D=512, mixed+learned vs FP64 plain at <=1e-8 E err"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=None)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--form", default=os.environ.get("PTN_BENCH_FORM", "mixed"),
+                   choices=["mixed", "fp64"])
+    p.add_argument("--L", type=int, default=64)
+    p.add_argument("--D", type=int, default=512)
+    p.add_argument("--m", type=int, default=10)
+    p.add_argument("--seed", type=int, default=2026)
+    p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--cpu-sites", type=int, default=3)
+    p.add_argument("--no-cpu", action="store_true")
+    p.add_argument("--no-accuracy", action="store_true")
+    p.add_argument("--graph", action="store_true")
+    a = p.parse_args()
+    if a.steps is None:
+        a.steps = 5 if a.form == "mixed" else 1
+    assert a.warmup >= 3, "at least 3 warm-up steps"
+    return a
+
+
+def workload_desc(a):
+    return (f"XXZ L={a.L} D={a.D} J=1 h=-0.1 Delta~U[0.5,1.5] (seed {a.seed}), "
+            f"dt=0.05j, numiter_lanczos={a.m}, one step = 2L-1 site updates")
+
+
+def make_workload(a, ptg_mod=None):
+    """Host-side inputs (seeded). Returns (mpo, psi, Delta); psi is not yet
+    orthonormalised."""
+    rng = np.random.default_rng(a.seed)
+    delta = float(rng.uniform(0.5, 1.5))
+    if ptg_mod is not None:
+        h = ptg_mod.heisenberg_xxz_1d_mpo(a.L, 1.0, delta, -0.1)
+        h.zero_qnumbers()
+        b = [min(2 ** min(i, a.L - i), a.D) for i in range(a.L + 1)]
+        psi = ptg_mod.MPS(h.qsite, [bi * [0] for bi in b], fill="random", rng=rng)
+        return h, psi, delta
+    from pytenet_gb300.hamiltonian import heisenberg_xxz_1d_mpo  # host-only module
+    h = heisenberg_xxz_1d_mpo(a.L, 1.0, delta, -0.1)
+    h.zero_qnumbers()
+    return h, None, delta
+
+
+# ------------------------------------------------------------------ CPU sample
+def cpu_sample(a, nsites_sample, rng_seed=7):
+    """Bounded sample of the same workload on the host cores with the NumPy
+    restatement of the reference algorithm: `nsites_sample` bulk site updates
+    (site expm with numiter applies, QR, left environment, bond expm, absorb) at
+    bond D with random environments of the right shapes. Returns seconds per
+    bulk site update and the sweep-average site-updates/s implied by the chain's
+    bond profile (cost ~ D_l * D_r * max(D_l, D_r) per site)."""
+    from oracle import ptn_oracle as orc
+    h, _, _ = make_workload(a)
+    D, d, m = a.D, 2, a.m
+    rng = np.random.default_rng(rng_seed)
+    w = h.a[a.L // 2]
+    chi = w.shape[0]
+
+    def herm_env():
+        x = orc.crandn((D, chi, D), rng) / D
+        return 0.5 * (x + x.conj().transpose(2, 1, 0))
+
+    l, r = herm_env(), herm_env()
+    aa = orc.crandn((D, d, D), rng)
+    aa /= np.linalg.norm(aa)
+    nxt = orc.crandn((D, d, D), rng)
+    dt = 0.05j
+    q0 = np.zeros(D * d, dtype=int)
+    q1 = np.zeros(D, dtype=int)
+    t0 = time.perf_counter()
+    for _ in range(nsites_sample):
+        x = orc._site_step(l, r, w, aa, 0.5 * dt, m)
+        q, c, _ = orc.block_sparse_qr(x.reshape(D * d, D), q0, q1)
+        x = q.reshape(D, d, D)
+        ln = orc.env_step_left(x, x, w, l)
+        c = orc._bond_step(ln, r, c, -0.5 * dt, m)
+        _ = np.tensordot(c, nxt, (1, 0))
+    sec = (time.perf_counter() - t0) / nsites_sample
+    b = [min(2 ** min(i, a.L - i), a.D) for i in range(a.L + 1)]
+    cost = [b[i] * b[i + 1] * max(b[i], b[i + 1]) for i in range(a.L)]
+    weights = np.array(cost, float) / float(D ** 3)
+    # L-1 sites in each direction plus the last site once: every site twice but one
+    sweep_units = 2.0 * weights.sum() - weights[-1]
+    sweep_sec = sweep_units * sec
+    return sec, (2 * a.L - 1) / sweep_sec
+
+
+def reference_arm(a):
+    """--impl reference: the reference's CPU algorithm (NumPy oracle port of
+    pytenet) on this host's cores, same metric and config, bounded sample per step."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count()
+    for _ in range(a.warmup):
+        cpu_sample(a, 1)
+    secs = []
+    for _ in range(a.steps):
+        s, _ = cpu_sample(a, 1)
+        secs.append(s)
+    sec = float(np.mean(secs))
+    b = [min(2 ** min(i, a.L - i), a.D) for i in range(a.L + 1)]
+    cost = [b[i] * b[i + 1] * max(b[i], b[i + 1]) for i in range(a.L)]
+    weights = np.array(cost, float) / float(a.D ** 3)
+    sweep_sec = (2.0 * weights.sum() - weights[-1]) * sec
+    value = (2 * a.L - 1) / sweep_sec
+    sample = (f"per step: 1 bulk site update (D={a.D}, random environments) of the NumPy "
+              f"restatement of pytenet's tdvp_singlesite; site-updates/s from the chain's "
+              f"bond profile (sweep = {2.0 * weights.sum() - weights[-1]:.1f} bulk-site units)")
+    out = {"metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": a.gpus,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": sweep_sec * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+           "data": "synthetic", "impl": "reference",
+           "config": {"workload": workload_desc(a), "l2": "inputs larger than L2"},
+           "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": cores,
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ our arm
+def our_arm(a):
+    import torch
+    import torch.distributed as dist
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    import __graft_entry__
+    __graft_entry__.build()
+    import pytenet_gb300 as ptg
+    from pytenet_gb300 import _lib
+    L = _lib.load()
+
+    h, psi, delta = make_workload(a, ptg)
+    psi.orthonormalize(mode="left")
+    psi_host0 = [x.copy() for x in psi.a]
+    qb0 = [q.copy() for q in psi.qbonds]
+    site_updates = 2 * a.L - 1
+
+    run = ptg.TDVPRun(h, psi, numiter_lanczos=a.m, precision=a.form, graph=a.graph)
+    dt = 0.05j
+    for _ in range(a.warmup):
+        run.step(dt)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    launches0 = L.ptn_launch_count()
+    dominant = 1 if a.form == "mixed" else 0
+    L.ptn_prof_start((1 << dominant) | (1 << 3))
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(a.steps):
+        run.step(dt)
+    e1.record()
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    L.ptn_prof_stop()
+    launches = L.ptn_launch_count() - launches0
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * site_updates * a.steps / (ms_max / 1e3)
+
+    def prof(kind):
+        import ctypes
+        tot, fl, by, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+        _lib.check(L.ptn_prof_read(kind, ctypes.byref(tot), ctypes.byref(fl), ctypes.byref(by),
+                                   ctypes.byref(n)))
+        return tot.value, fl.value, by.value, n.value
+
+    k_ms, k_fl, k_by, k_n = prof(dominant)
+    q_ms, q_fl, q_by, q_n = prof(3)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    if dominant == 1:
+        peak = peaks.get("bf16_tflops", 1900.0)
+        peak_src = "bf16_tflops of measured" if "bf16_tflops" in peaks else "bf16 of fallback"
+        achieved = k_fl / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
+        unit = "TFLOP/s"
+        kern = "tcgen05 split-BF16 complex GEMM"
+    else:
+        # FP64 tensor (DMMA) peak: measured on this machine's GB300 with a DMMA-only kernel
+        peak = 1.047
+        peak_src = "FP64 DMMA m8n8k4 throughput measured on GB300 (1.047 TFLOP/s)"
+        achieved = k_fl / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
+        unit = "TFLOP/s"
+        kern = "DMMA complex128 GEMM"
+    roofline = {"bound": "tensor", "kernel": kern, "achieved": achieved, "peak": peak,
+                "unit": unit, "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "peak_source": peak_src, "launches_timed": k_n,
+                "kernel_share_of_step": (k_ms / ms) if ms > 0 else None,
+                "qr_share_of_step": (q_ms / ms) if ms > 0 else None,
+                "flops_per_launch": (k_fl / k_n) if k_n else None}
+
+    # ---- accuracy of the mixed form vs the FP64 form (same initial state)
+    accuracy = None
+    if a.form == "mixed" and not a.no_accuracy and rank == 0:
+        accuracy = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, run)
+
+    # ---- e2e through the public API with host buffers
+    e2e = None
+    if a.e2e_steps > 0:
+        psi_e = ptg.MPS(psi.qsite, qb0, fill="postpone")
+        psi_e.a = [x.copy() for x in psi_host0]
+        h2d = sum(x.nbytes for x in psi_e.a) + sum(np.asarray(w, complex).nbytes for w in h.a)
+        d2h = sum(x.nbytes for x in psi_e.a)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(a.e2e_steps):
+            ptg.tdvp_singlesite(h, psi_e, dt, 1, numiter_lanczos=a.m, precision=a.form)
+        torch.cuda.synchronize()
+        et = time.perf_counter() - t0
+        e2e = {"value": world * site_updates * a.e2e_steps / et, "unit": "site-updates/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "steps": a.e2e_steps,
+               "what": "tdvp_singlesite(hamiltonian, psi_host, dt, numsteps=1) per step: "
+                       "upload, right-normalisation, environments, one step, download"}
+
+    cpu = None
+    if rank == 0 and world == 1 and not a.no_cpu:
+        sec, rate = cpu_sample(a, a.cpu_sites)
+        cpu = {"value": rate, "unit": "site-updates/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{a.cpu_sites} bulk site updates at D={a.D} ({sec:.2f} s each) of the "
+                         f"NumPy restatement of pytenet's tdvp_singlesite on all host cores; "
+                         f"sweep-average rate from the chain's bond profile"}
+
+    if rank == 0:
+        out = {"metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
+               "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+               "dtype": "c128" if a.form == "fp64" else "split-bf16 (fp32 acc) + fp64 krylov/qr",
+               "data": "synthetic",
+               "config": {"workload": workload_desc(a), "form": a.form, "L": a.L, "D": a.D,
+                          "numiter_lanczos": a.m, "delta": delta, "graph": a.graph,
+                          "parallelism": f"replicas x{world}",
+                          "l2": "inputs larger than L2 (state of several GB per replica)"},
+               "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+               "cpu_baseline": cpu, "accuracy_vs_fp64": accuracy}
+        print(json.dumps(out))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, run_mixed):
+    """Energy / fidelity of the mixed run vs the FP64 run from the same state."""
+    from pytenet_gb300.chain_ops import mpo_average, mps_vdot, mps_norm
+    nsteps = run_mixed.steps_done
+    psi_m = ptg.MPS(ptg.MPS(h.qsite, qb0, fill="postpone").qsite, qb0, fill="postpone")
+    run_mixed.chain.download(psi_m)
+    psi_f = ptg.MPS(h.qsite, qb0, fill="postpone")
+    psi_f.a = [x.copy() for x in psi_host0]
+    rf = ptg.TDVPRun(h, psi_f, numiter_lanczos=a.m, precision="fp64")
+    for _ in range(nsteps):
+        rf.step(0.05j)
+    rf.download()
+    e_m, e_f = mpo_average(psi_m, h).real, mpo_average(psi_f, h).real
+    ov = mps_vdot(psi_f, psi_m)
+    nm, nf = mps_norm(psi_m), mps_norm(psi_f)
+    return {"steps": nsteps, "energy_fp64": e_f, "energy_mixed": e_m,
+            "energy_rel_err": abs(e_m - e_f) / max(abs(e_f), 1e-300),
+            "infidelity": 1.0 - abs(ov) ** 2 / (nm * nm * nf * nf),
+            "norm_drift": abs(nm - nf)}
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        reference_arm(a)
+    else:
+        our_arm(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -77,6 +77,15 @@ const char* ptn_version(void);
 const char* ptn_last_error(void);
 /* number of kernel launches issued by this library since load (diagnostics) */
 uint64_t ptn_launch_count(void);
+/* Live kernel timing. ptn_prof_start(mask) clears the record and, for every
+ * kind k with bit k set (0 FP64 GEMM, 1 tensor-core GEMM, 2 MPO stage, 3 QR,
+ * 4 Krylov passes), brackets each launch with CUDA events on its stream (not
+ * while a stream is being captured). After synchronising, ptn_prof_read sums
+ * the event intervals, the algorithmic flops and bytes and the launch count. */
+void ptn_prof_start(unsigned kind_mask);
+void ptn_prof_stop(void);
+ptn_status ptn_prof_read(int kind, double* total_ms, double* flops, double* bytes,
+                         long* launches);
 
 /* ----------------------------------------------------------- contractions */
 

@@ -66,6 +66,9 @@ _SIGS = {
     "ptn_version": (C.c_char_p, []),
     "ptn_last_error": (C.c_char_p, []),
     "ptn_launch_count": (C.c_uint64, []),
+    "ptn_prof_start": (None, [C.c_uint]),
+    "ptn_prof_stop": (None, []),
+    "ptn_prof_read": (I, [I, C.POINTER(D), C.POINTER(D), C.POINTER(D), C.POINTER(L)]),
     "ptn_heff_workspace_bytes": (S, [I, I, I, I, I, I]),
     "ptn_heff_apply": (I, [P, P, P, P, P, I, I, I, I, I, I, P, S, P]),
     "ptn_bond_workspace_bytes": (S, [I, I, I, I]),

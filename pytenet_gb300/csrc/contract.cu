@@ -237,6 +237,11 @@ ptn_status heff_apply_mixed_entry(const double2*, const double2*, const double2*
                                   double2*, int, int, int, int, int, void*, size_t, cudaStream_t);
 ptn_status bond_apply_mixed_entry(const double2*, const double2*, const double2*, double2*, int,
                                   int, int, void*, size_t, cudaStream_t);
+size_t env_workspace_bytes_mixed(int Dl, int d, int Dr, int cl, int cr);
+ptn_status env_left_mixed(const double2*, const double2*, const double2*, const double2*, double2*,
+                          int, int, int, int, int, void*, size_t, cudaStream_t);
+ptn_status env_right_mixed(const double2*, const double2*, const double2*, const double2*, double2*,
+                           int, int, int, int, int, void*, size_t, cudaStream_t);
 }  // namespace ptn
 
 extern "C" {
@@ -252,8 +257,8 @@ size_t ptn_bond_workspace_bytes(int Dl, int Dr, int chi, int prec) {
 }
 
 size_t ptn_env_workspace_bytes(int Dl, int d, int Dr, int chil, int chir, int prec) {
-  (void)prec;  // environments are always accumulated in FP64
-  return env_workspace_bytes_f64(Dl, d, Dr, chil, chir);
+  return prec == PTN_PREC_FP64 ? env_workspace_bytes_f64(Dl, d, Dr, chil, chir)
+                               : env_workspace_bytes_mixed(Dl, d, Dr, chil, chir);
 }
 
 ptn_status ptn_heff_apply(const ptn_c128* a, const ptn_c128* w, const ptn_c128* l,
@@ -282,7 +287,9 @@ ptn_status ptn_env_step_left(const ptn_c128* a, const ptn_c128* b, const ptn_c12
                              const ptn_c128* l, ptn_c128* l_next, int Dl, int d, int Dr, int chil,
                              int chir, int prec, void* ws, size_t ws_bytes, void* stream) {
   PTN_CHECK_ARG(Dl > 0 && d > 0 && Dr > 0 && chil > 0 && chir > 0, "env_left: bad dims");
-  (void)prec;  // environments are always accumulated in FP64
+  if (prec != PTN_PREC_FP64)
+    return env_left_mixed(D2(a), D2(b), D2(w), D2(l), D2(l_next), Dl, d, Dr, chil, chir, ws,
+                          ws_bytes, as_stream(stream));
   return env_left_f64(D2(a), D2(b), D2(w), D2(l), D2(l_next), Dl, d, Dr, chil, chir, ws, ws_bytes,
                       as_stream(stream));
 }
@@ -291,7 +298,9 @@ ptn_status ptn_env_step_right(const ptn_c128* a, const ptn_c128* b, const ptn_c1
                               const ptn_c128* r, ptn_c128* r_next, int Dl, int d, int Dr, int chil,
                               int chir, int prec, void* ws, size_t ws_bytes, void* stream) {
   PTN_CHECK_ARG(Dl > 0 && d > 0 && Dr > 0 && chil > 0 && chir > 0, "env_right: bad dims");
-  (void)prec;
+  if (prec != PTN_PREC_FP64)
+    return env_right_mixed(D2(a), D2(b), D2(w), D2(r), D2(r_next), Dl, d, Dr, chil, chir, ws,
+                           ws_bytes, as_stream(stream));
   return env_right_f64(D2(a), D2(b), D2(w), D2(r), D2(r_next), Dl, d, Dr, chil, chir, ws, ws_bytes,
                        as_stream(stream));
 }

@@ -36,6 +36,38 @@ int num_sms() {
   return cached;
 }
 
+// ------------------------------------------------------------------ live timing
+namespace {
+constexpr int PROF_SLOTS = 1 << 15;
+struct ProfSlot {
+  cudaEvent_t a = nullptr, b = nullptr;
+  int kind = 0;
+  double flops = 0, bytes = 0;
+};
+ProfSlot g_prof[PROF_SLOTS];
+int g_prof_used = 0;
+unsigned g_prof_mask = 0;
+}  // namespace
+
+int prof_begin(cudaStream_t st, int kind, double flops, double bytes) {
+  if (!(g_prof_mask & (1u << kind)) || g_prof_used >= PROF_SLOTS) return -1;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return -1;
+  ProfSlot& p = g_prof[g_prof_used];
+  if (p.a == nullptr) {
+    if (cudaEventCreate(&p.a) != cudaSuccess || cudaEventCreate(&p.b) != cudaSuccess) return -1;
+  }
+  p.kind = kind;
+  p.flops = flops;
+  p.bytes = bytes;
+  if (cudaEventRecord(p.a, st) != cudaSuccess) return -1;
+  return g_prof_used++;
+}
+
+void prof_end(cudaStream_t st, int slot) {
+  if (slot >= 0) cudaEventRecord(g_prof[slot].b, st);
+}
+
 namespace {
 
 int grid_for(long n, int threads = 256) {
@@ -156,6 +188,34 @@ int ptn_abi_version(void) { return PTN_ABI_VERSION; }
 const char* ptn_version(void) { return "pytenet_gb300 0.1 (sm_103a)"; }
 const char* ptn_last_error(void) { return g_err; }
 uint64_t ptn_launch_count(void) { return g_launches.load(); }
+
+void ptn_prof_start(unsigned kind_mask) {
+  g_prof_used = 0;
+  g_prof_mask = kind_mask;
+}
+
+ptn_status ptn_prof_read(int kind, double* total_ms, double* flops, double* bytes,
+                         long* launches) {
+  double ms = 0, fl = 0, by = 0;
+  long n = 0;
+  for (int i = 0; i < g_prof_used; ++i) {
+    ProfSlot& p = g_prof[i];
+    if (p.kind != kind) continue;
+    float t = 0.f;
+    PTN_CUDA_TRY(cudaEventElapsedTime(&t, p.a, p.b));
+    ms += t;
+    fl += p.flops;
+    by += p.bytes;
+    ++n;
+  }
+  *total_ms = ms;
+  *flops = fl;
+  *bytes = by;
+  *launches = n;
+  return PTN_OK;
+}
+
+void ptn_prof_stop(void) { g_prof_mask = 0; }
 
 ptn_status ptn_gather(const ptn_c128* src, const int64_t* row_off, const int64_t* col_off, int nr,
                       int nc, ptn_c128* dst, void* stream) {

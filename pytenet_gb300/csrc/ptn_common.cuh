@@ -44,6 +44,17 @@ inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s
 int num_sms();
 
 // ---------------------------------------------------------------------------
+// live kernel timing (off by default): launchers bracket a kernel of `kind`
+// with CUDA events on its stream and record the algorithmic flops / bytes of
+// the launch; ptn_prof_read sums the event intervals after a synchronise.
+// Nothing is recorded while the stream is being captured into a graph.
+// ---------------------------------------------------------------------------
+enum ProfKind { PROF_ZGEMM_F64 = 0, PROF_TC_GEMM = 1, PROF_MPO_STAGE = 2, PROF_QR = 3,
+                PROF_KRYLOV = 4, PROF_NKINDS = 5 };
+int prof_begin(cudaStream_t st, int kind, double flops, double bytes);
+void prof_end(cudaStream_t st, int slot);
+
+// ---------------------------------------------------------------------------
 // complex helpers
 // ---------------------------------------------------------------------------
 __host__ __device__ __forceinline__ double2 c2(double re, double im) { return make_double2(re, im); }

@@ -345,6 +345,9 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
   const int k = std::min(m, n);
   QrWs w = carve_qr(ws, m, n);
   const long lda = n;
+  // LAPACK flop count of zgeqrf + zungqr (4 real flops per complex op)
+  const double fq = 8.0 * ((double)m * n * k - (double)(m + n) * k * k / 2.0 + (double)k * k * k / 3.0);
+  const int prof = prof_begin(st, PROF_QR, 2.0 * fq, 16.0 * 3.0 * m * n);
   for (int j0 = 0, p = 0; j0 < k; j0 += NB, ++p) {
     const int jb = std::min(NB, k - j0);
     qr_panel_kernel<<<1, PT, 0, st>>>(a, lda, m, j0, jb, w.T + (long)p * NB * NB, w.V, k);
@@ -368,6 +371,7 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
     PTN_TRY(larfb(q, ldq, w.V, k, j0, m, j0, k - j0, j0, jb, w.T + (long)p * NB * NB, false,
                   w.part, st));
   }
+  prof_end(st, prof);
   return PTN_OK;
 }
 

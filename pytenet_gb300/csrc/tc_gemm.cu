@@ -1,0 +1,475 @@
+// Split-BF16 complex GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+//
+// A complex product C = op(A) op(B) is computed as one real GEMM on BF16 slices
+// with FP32 accumulation in tensor memory:
+//   - every FP64 value x is split into three BF16 slices x = x0 + x1 + x2 (8
+//     significant bits each, ~24 bits together);
+//   - the "plain" operand A is the row-major complex matrix read as real
+//     (M x 2K: re/im interleaved along K), the "embedded" operand B holds each
+//     complex entry z as the 2x2 real block [[Re z, -Im z], [Im z, Re z]]
+//     (2N x 2K, K-major), so that the real product (M x 2N) is the complex
+//     product with re/im interleaved -- i.e. the complex128 output layout;
+//   - the slice products sum_{i+j<=2} A_i B_j (six pairs, smallest first) are
+//     accumulated in one FP32 tensor-memory accumulator; long K is split across
+//     CTAs whose FP32 partials are summed in FP64.
+//
+// Kernel: one 128 x 256 output tile per CTA (UMMA M=128, N=256, K=16), BK=64
+// (one 128-byte swizzle atom of BF16), 4-stage TMA -> shared memory pipeline with
+// full/empty mbarriers. Warp 0 lane 0 issues TMA, warp 1 lane 0 issues
+// tcgen05.mma and tcgen05.commit, warps 2..5 read the accumulator back with
+// tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..) and write FP64 complex results
+// (or FP32 split-K partials). Every mbarrier wait is bounded: on expiry the
+// kernel records an error code, stops issuing work and still frees its TMEM.
+#include "ptn_common.cuh"
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+namespace ptn {
+
+void note_launches(int n);
+
+namespace {
+
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 4;
+constexpr int A_TILE = BM * BK * 2;
+constexpr int B_TILE = BN * BK * 2;
+constexpr int STAGE_BYTES = A_TILE + B_TILE;
+constexpr int THREADS = 192;
+constexpr int TMEM_COLS = 256;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr long WAIT_LIMIT = 1L << 24;
+// kind::f16 instruction descriptor: FP32 accumulate (bit 4), A and B BF16
+// (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+struct TcArgs {
+  int M, N;            // output rows, real output columns (2 x complex columns)
+  int nkb;             // K blocks (of BK) per slice pair
+  int npairs;
+  int pa[8], pb[8];    // slice indices per pair
+  int it_per_split, splits;
+  double2* out;        // complex output element (m, c) at out[m * ldm + c * ldn]
+  long ldm, ldn;
+  int accumulate;      // out += result instead of out = result
+  float* part;         // split-K partials [splits][M][N], or null
+  int* err;
+  const int* skip;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+// bounded wait on the phase with parity `parity`; false on expiry
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  const uint32_t a = smem_u32(bar);
+  for (long it = 0; it < WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int x, int y, int z,
+                                            uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1 << 16;
+  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)1 << 46;
+  d |= (uint64_t)2 << 61;
+  return d;
+}
+
+__device__ __forceinline__ void umma(uint32_t tmem, uint64_t ad, uint64_t bd, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+      " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
+      "l"(ad), "l"(bd), "r"(IDESC), "r"(acc)
+      : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                   smem_u32(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
+      " [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
+        "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(THREADS, 1)
+    tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                   const TcArgs p) {
+  if (p.skip != nullptr && *p.skip != 0) return;  // uniform: before any barrier or allocation
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * A_TILE;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfull + 1);
+  int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
+  const int split = blockIdx.z;
+  const int total = p.npairs * p.nkb;
+  const int it0 = split * p.it_per_split;
+  const int it1 = min(total, it0 + p.it_per_split);
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer
+    int issued = 0;
+    for (int it = it0, i = 0; it < it1; ++it, ++i) {
+      const int s = i % STAGES;
+      const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+      if (i >= STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
+        atomicExch(p.err, 1);
+        *(volatile int*)abort_flag = 1;
+        break;
+      }
+      if (*(volatile int*)abort_flag) break;
+      const int pr = it / p.nkb, kb = it % p.nkb;
+      mbar_expect_tx(&full[s], STAGE_BYTES);
+      tma_load_3d(sA + s * A_TILE, &tmA, kb * BK, m0, p.pa[pr], &full[s]);
+      tma_load_3d(sB + s * B_TILE, &tmB, kb * BK, n0, p.pb[pr], &full[s]);
+      ++issued;
+    }
+    if (*(volatile int*)abort_flag) {
+      // drain: let the copies still in flight land before the CTA retires (bounded)
+      for (int i = max(0, issued - STAGES); i < issued; ++i)
+        mbar_wait(&full[i % STAGES], (uint32_t)(i / STAGES) & 1u);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer
+    int issued = 0;
+    for (int it = it0, i = 0; it < it1; ++it, ++i) {
+      const int s = i % STAGES;
+      const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+      if (!mbar_wait(&full[s], ph)) {
+        atomicExch(p.err, 2);
+        *(volatile int*)abort_flag = 1;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t a0 = smem_u32(sA + s * A_TILE), b0 = smem_u32(sB + s * B_TILE);
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k)
+        umma(tmem, sdesc(a0 + k * 32), sdesc(b0 + k * 32), (i > 0 || k > 0) ? 1u : 0u);
+      umma_commit(&empty[s]);
+      ++issued;
+    }
+    if (issued > 0) umma_commit(tfull);
+    else mbar_arrive(tfull);
+  } else if (warp >= 2) {
+    // ---------------- epilogue: TMEM -> registers -> global
+    const bool ok = mbar_wait(tfull, 0);
+    if (!ok) atomicExch(p.err, 3);
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const int g = warp & 3;
+    const int row = m0 + 32 * g + lane;
+    const bool have = ok && (it1 > it0) && !*(volatile int*)abort_flag;
+    for (int c0 = 0; c0 < BN; c0 += 16) {
+      uint32_t v[16];
+      tmem_ld16(tmem + ((uint32_t)(32 * g) << 16) + (uint32_t)c0, v);
+      if (row >= p.M) continue;
+#pragma unroll
+      for (int j = 0; j < 16; j += 2) {
+        const int col = n0 + c0 + j;
+        if (col >= p.N) continue;
+        const float re = have ? __uint_as_float(v[j]) : 0.f;
+        const float im = have ? __uint_as_float(v[j + 1]) : 0.f;
+        if (p.part != nullptr) {
+          float2* dst = reinterpret_cast<float2*>(p.part + ((long)split * p.M + row) * p.N + col);
+          *dst = make_float2(re, im);
+        } else {
+          double2* o = p.out + (long)row * p.ldm + (long)(col >> 1) * p.ldn;
+          double2 x = make_double2((double)re, (double)im);
+          if (p.accumulate) {
+            const double2 y = *o;
+            x.x += y.x;
+            x.y += y.y;
+          }
+          *o = x;
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
+__global__ void splitk_sum_kernel(const float* __restrict__ part, int splits, int M, int N,
+                                  double2* __restrict__ out, long ldm, long ldn, int accumulate,
+                                  const int* skip) {
+  if (skip != nullptr && *skip != 0) return;
+  const int nc = N >> 1;
+  const long total = (long)M * nc;
+  for (long idx = blockIdx.x * (long)blockDim.x + threadIdx.x; idx < total;
+       idx += (long)gridDim.x * blockDim.x) {
+    // consecutive threads take consecutive rows: the complex outputs of the
+    // transposed-output GEMMs are then written contiguously
+    const int m = (int)(idx % M), c = (int)(idx / M);
+    double re = 0.0, im = 0.0;
+    for (int s = 0; s < splits; ++s) {
+      const float2 v = *reinterpret_cast<const float2*>(part + ((long)s * M + m) * N + 2 * c);
+      re += (double)v.x;
+      im += (double)v.y;
+    }
+    double2* o = out + (long)m * ldm + (long)c * ldn;
+    if (accumulate) {
+      const double2 y = *o;
+      re += y.x;
+      im += y.y;
+    }
+    *o = make_double2(re, im);
+  }
+}
+
+// ------------------------------------------------------------------ tensor maps
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+  });
+  return fn;
+}
+
+struct MapKey {
+  const void* ptr;
+  long rows, K, Kp, plane;
+  int box_rows;
+  bool operator==(const MapKey& o) const {
+    return ptr == o.ptr && rows == o.rows && K == o.K && Kp == o.Kp && plane == o.plane &&
+           box_rows == o.box_rows;
+  }
+};
+
+struct MapCache {
+  std::vector<std::pair<MapKey, CUtensorMap>> entries;
+  std::mutex mu;
+};
+
+MapCache& map_cache() {
+  static MapCache c;
+  return c;
+}
+
+// 3-D map over slices [3][rows][Kp] of BF16, logical extent (K, rows, 3), box (64, box_rows, 1)
+bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, long plane,
+              int box_rows) {
+  MapKey key{ptr, rows, K, Kp, plane, box_rows};
+  MapCache& c = map_cache();
+  {
+    std::lock_guard<std::mutex> lk(c.mu);
+    for (auto& e : c.entries)
+      if (e.first == key) {
+        *out = e.second;
+        return true;
+      }
+  }
+  EncodeTiledFn fn = encode_fn();
+  if (fn == nullptr) return false;
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
+  cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)plane * 2};
+  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUtensorMap m;
+  CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(ptr), dims, strides,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return false;
+  std::lock_guard<std::mutex> lk(c.mu);
+  if (c.entries.size() > 512) c.entries.clear();
+  c.entries.push_back({key, m});
+  *out = m;
+  return true;
+}
+
+// sticky error code of the tensor-core kernels (bounded waits that expired)
+__device__ int g_tc_err;
+
+int* err_flag() {
+  static int* flag = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* a = nullptr;
+    if (cudaGetSymbolAddress(&a, g_tc_err) == cudaSuccess) flag = static_cast<int*>(a);
+  });
+  return flag;
+}
+
+}  // namespace
+
+// Slice-pair schedule of the split-BF16 product, smallest terms first.
+static const int kPairA[6] = {2, 1, 0, 1, 0, 0};
+static const int kPairB[6] = {0, 1, 2, 0, 1, 0};
+
+size_t tc_gemm_workspace_bytes(int M, int Ncomplex, int Kcomplex) {
+  const int N = 2 * Ncomplex, K = 2 * Kcomplex;
+  const int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  const int nkb = (K + BK - 1) / BK;
+  const int total = 6 * nkb;
+  int splits = 1;
+  const int target = 2 * num_sms();
+  if (tiles < target) splits = std::max(1, std::min((target + tiles - 1) / tiles, total / 8));
+  return splits > 1 ? (size_t)splits * M * N * sizeof(float) : 0;
+}
+
+// C (M x Nc complex) = A (M x Kc) * B (Kc x Nc) from slice buffers:
+//   Aslices: [3][M][Kp] BF16 (plain), Bslices: [3][2 Nc][Kp] BF16 (embedded), Kp >= 2 Kc, Kp % 8 == 0.
+ptn_status tc_gemm(const void* Aslices, long aplane, const void* Bslices, long bplane, int M,
+                   int Nc, int Kc, long Kp, double2* out, long ldm, long ldn, bool accumulate,
+                   void* ws, size_t ws_bytes, const int* skip, cudaStream_t st) {
+  const int N = 2 * Nc, K = 2 * Kc;
+  PTN_CHECK_ARG(M > 0 && Nc > 0 && Kc > 0 && Kp >= K && Kp % 8 == 0, "tc_gemm: bad sizes");
+  PTN_CHECK_ARG(reinterpret_cast<uintptr_t>(Aslices) % 16 == 0 &&
+                    reinterpret_cast<uintptr_t>(Bslices) % 16 == 0,
+                "tc_gemm: slice buffers must be 16-byte aligned");
+  CUtensorMap ma, mb;
+  if (!make_map(&ma, Aslices, M, K, Kp, aplane, BM) || !make_map(&mb, Bslices, N, K, Kp, bplane, BN)) {
+    set_error("tc_gemm: cuTensorMapEncodeTiled failed");
+    return PTN_CUDA_ERROR;
+  }
+  static bool attr = false;
+  if (!attr) {
+    PTN_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SMEM_BYTES));
+    attr = true;
+  }
+  TcArgs a;
+  a.M = M;
+  a.N = N;
+  a.nkb = (K + BK - 1) / BK;
+  a.npairs = 6;
+  for (int i = 0; i < 6; ++i) { a.pa[i] = kPairA[i]; a.pb[i] = kPairB[i]; }
+  const int total = a.npairs * a.nkb;
+  const int gx = (N + BN - 1) / BN, gy = (M + BM - 1) / BM;
+  int splits = 1;
+  const int target = 2 * num_sms();
+  if (gx * gy < target) splits = std::max(1, std::min((target + gx * gy - 1) / (gx * gy), total / 8));
+  while (splits > 1 && (size_t)splits * M * N * sizeof(float) > ws_bytes) --splits;
+  a.it_per_split = (total + splits - 1) / splits;
+  splits = (total + a.it_per_split - 1) / a.it_per_split;   // no empty split
+  a.splits = splits;
+  a.out = out;
+  a.ldm = ldm;
+  a.ldn = ldn;
+  a.accumulate = accumulate ? 1 : 0;
+  a.part = splits > 1 ? static_cast<float*>(ws) : nullptr;
+  a.err = err_flag();
+  a.skip = skip;
+  PTN_CHECK_ARG(a.err != nullptr, "tc_gemm: error flag lookup failed");
+  PTN_CHECK_ARG(gy <= 65535 && splits <= 65535, "tc_gemm: grid too large");
+  const int prof = prof_begin(st, PROF_TC_GEMM, 8.0 * M * (double)Nc * Kc,
+                              2.0 * 3 * ((double)M * Kp + (double)N * Kp) + 16.0 * M * Nc);
+  tc_gemm_kernel<<<dim3(gx, gy, splits), THREADS, SMEM_BYTES, st>>>(ma, mb, a);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  if (splits > 1) {
+    const long tot = (long)M * Nc;
+    const int blocks = (int)std::min<long>((tot + 255) / 256, 8L * num_sms());
+    splitk_sum_kernel<<<blocks, 256, 0, st>>>(a.part, splits, M, N, out, ldm, ldn, a.accumulate,
+                                              skip);
+    PTN_LAUNCH_CHECK();
+    note_launches(1);
+  }
+  prof_end(st, prof);
+  return PTN_OK;
+}
+
+// host read of the sticky error flag (0 = fine); resets it
+int tc_gemm_error_and_reset() {
+  int v = 0;
+  if (cudaMemcpyFromSymbol(&v, g_tc_err, sizeof(int)) != cudaSuccess) return -1;
+  if (v != 0) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_tc_err, &zero, sizeof(int));
+  }
+  return v;
+}
+
+}  // namespace ptn

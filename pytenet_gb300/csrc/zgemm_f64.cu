@@ -285,6 +285,8 @@ ptn_status zgemm(const GemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st) 
   k.part = splits > 1 ? static_cast<double2*>(ws) : nullptr;
   dim3 grid((g.N + BN - 1) / BN, (g.M + BM - 1) / BM, g.batch * splits);
   PTN_CHECK_ARG(grid.y <= 65535 && grid.z <= 65535, "zgemm: grid too large");
+  const int prof = prof_begin(st, PROF_ZGEMM_F64, 8.0 * g.M * g.N * (double)g.K * g.batch,
+                              16.0 * g.batch * ((double)g.M * g.K + (double)g.K * g.N + 2.0 * g.M * g.N));
   switch (oa) {
     case OP_N: launch_b<OP_N>(ob, grid, st, k); break;
     case OP_T: launch_b<OP_T>(ob, grid, st, k); break;
@@ -300,6 +302,7 @@ ptn_status zgemm(const GemmArgs& g, void* ws, size_t ws_bytes, cudaStream_t st) 
     PTN_LAUNCH_CHECK();
     note_launches(1);
   }
+  prof_end(st, prof);
   return PTN_OK;
 }
 

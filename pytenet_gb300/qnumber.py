@@ -42,7 +42,7 @@ def is_qsparse(a, qnums):
     mask = qnumber_outer_sum(qnums) != 0
     if hasattr(a, "is_cuda"):
         import torch
-        m = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(mask, tuple(a.shape)))).to(a.device)
+        m = torch.from_numpy(np.array(np.broadcast_to(mask, tuple(a.shape)))).to(a.device)
         return not bool(torch.any(a[m] != 0).item())
     a = np.asarray(a)
     return not np.any(np.where(mask, a, 0))
