@@ -128,6 +128,17 @@ ptn_status ptn_zgemm(char opA, char opB, int M, int N, int K, ptn_c128 alpha,
                      long strideB, ptn_c128 beta, ptn_c128* C, long ldc, long strideC,
                      int batch, void* ws, size_t ws_bytes, void* stream);
 
+/* C = A B for row-major complex A (M x K, leading dim lda) and B (K x N, ldb) on the
+ * tensor cores: split-BF16 products with FP32 accumulation (the arithmetic of
+ * PTN_PREC_SPLIT_BF16), FP64 output. */
+size_t ptn_zgemm_split_bf16_workspace_bytes(int M, int N, int K);
+ptn_status ptn_zgemm_split_bf16(const ptn_c128* A, long lda, const ptn_c128* B, long ldb,
+                                ptn_c128* C, long ldc, int M, int N, int K, void* ws,
+                                size_t ws_bytes, void* stream);
+/* Sticky error code of the tensor-core kernels (1-3: a bounded wait expired in
+ * the producer / MMA / epilogue role), then reset to 0. Synchronises the device. */
+int ptn_tc_error(void);
+
 /* ------------------------------------------------------------ Krylov core
  * lanczos_iteration / expm_krylov / eigh_krylov, pytenet/krylov.py:12-150.
  * The caller owns `V`, a (maxiter, n) complex buffer of Lanczos vectors, and a

@@ -79,6 +79,9 @@ _SIGS = {
     "ptn_zgemm_workspace_bytes": (S, [I, I, I, I]),
     "ptn_zgemm": (I, [C.c_char, C.c_char, I, I, I, c128, P, L, L, P, L, L, c128, P, L, L, I, P, S,
                       P]),
+    "ptn_zgemm_split_bf16_workspace_bytes": (S, [I, I, I]),
+    "ptn_zgemm_split_bf16": (I, [P, L, P, L, P, L, I, I, I, P, S, P]),
+    "ptn_tc_error": (I, []),
     "ptn_krylov_state_bytes": (S, []),
     "ptn_krylov_stop_flag": (P, [P]),
     "ptn_krylov_start": (I, [P, P, P, L, I, P]),

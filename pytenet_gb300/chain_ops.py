@@ -63,8 +63,10 @@ def apply_local_bond_contraction(c, l, r, precision="fp64"):
     return _ret(out, host)
 
 
-def contraction_operator_step_left(a, b, w, l):
+def contraction_operator_step_left(a, b, w, l, precision="fp64"):
     """Left environment step (pytenet/chain_ops.py:60-99): l_next[r_a, chi_r, r_b]."""
+    from .engine import prec_code
+    p = prec_code(precision)
     assert a.ndim == 3 and b.ndim == 3 and w.ndim == 4 and l.ndim == 3
     assert tuple(a.shape) == tuple(b.shape), "a and b must have equal shapes"
     host = _is_host(a, b, w, l)
@@ -74,14 +76,16 @@ def contraction_operator_step_left(a, b, w, l):
     A, B, W, Lt = (to_dev(x) for x in (a, b, w, l))
     out = empty((Dr, cr, Dr))
     L = lib()
-    wsb = L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, 0)
-    call(L.ptn_env_step_left, ptr(A), ptr(B), ptr(W), ptr(Lt), ptr(out), Dl, d, Dr, cl, cr, 0,
+    wsb = L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, p)
+    call(L.ptn_env_step_left, ptr(A), ptr(B), ptr(W), ptr(Lt), ptr(out), Dl, d, Dr, cl, cr, p,
          ptr(_WS.get(wsb)), wsb, stream_ptr())
     return _ret(out, host)
 
 
-def contraction_operator_step_right(a, b, w, r):
+def contraction_operator_step_right(a, b, w, r, precision="fp64"):
     """Right environment step (pytenet/chain_ops.py:16-57): r_next[l_a, chi_l, l_b]."""
+    from .engine import prec_code
+    p = prec_code(precision)
     assert a.ndim == 3 and b.ndim == 3 and w.ndim == 4 and r.ndim == 3
     assert tuple(a.shape) == tuple(b.shape), "a and b must have equal shapes"
     host = _is_host(a, b, w, r)
@@ -91,8 +95,8 @@ def contraction_operator_step_right(a, b, w, r):
     A, B, W, R = (to_dev(x) for x in (a, b, w, r))
     out = empty((Dl, cl, Dl))
     L = lib()
-    wsb = L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, 0)
-    call(L.ptn_env_step_right, ptr(A), ptr(B), ptr(W), ptr(R), ptr(out), Dl, d, Dr, cl, cr, 0,
+    wsb = L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, p)
+    call(L.ptn_env_step_right, ptr(A), ptr(B), ptr(W), ptr(R), ptr(out), Dl, d, Dr, cl, cr, p,
          ptr(_WS.get(wsb)), wsb, stream_ptr())
     return _ret(out, host)
 

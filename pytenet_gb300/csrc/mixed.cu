@@ -461,4 +461,49 @@ ptn_status env_right_mixed(const double2* a, const double2* b, const double2* w,
   return PTN_OK;
 }
 
+// ================================================================ plain GEMM entry
+size_t zgemm_split_workspace_bytes(int M, int N, int K) {
+  Carver c(nullptr);
+  take_slices(c, M, K);
+  take_slices(c, 2L * N, K);
+  c.take(tc_gemm_workspace_bytes(M, N, K));
+  return c.off;
+}
+
+// C = A B (row-major complex, M x K times K x N) through split-BF16 tensor-core products
+ptn_status zgemm_split(const double2* A, long lda, const double2* B, long ldb, double2* C, long ldc,
+                       int M, int N, int K, void* ws, size_t ws_bytes, cudaStream_t st) {
+  PTN_CHECK_ARG(M > 0 && N > 0 && K > 0, "zgemm_split: bad sizes");
+  PTN_CHECK_ARG(ws_bytes >= zgemm_split_workspace_bytes(M, N, K), "zgemm_split: workspace too small");
+  Carver c(ws);
+  Slices As = take_slices(c, M, K);
+  Slices Bs = take_slices(c, 2L * N, K);
+  const size_t gb = tc_gemm_workspace_bytes(M, N, K);
+  void* g = c.take(gb);
+  PTN_TRY(plain(A, lda, 1, As, false, nullptr, st));
+  PTN_TRY(embed(B, 1, ldb, N, Bs, false, nullptr, st));
+  return gemm(As, Bs, M, N, K, C, ldc, 1, g, gb, nullptr, st);
+}
+
 }  // namespace ptn
+
+extern "C" {
+
+size_t ptn_zgemm_split_bf16_workspace_bytes(int M, int N, int K) {
+  return ptn::zgemm_split_workspace_bytes(M, N, K);
+}
+
+ptn_status ptn_zgemm_split_bf16(const ptn_c128* A, long lda, const ptn_c128* B, long ldb,
+                                ptn_c128* C, long ldc, int M, int N, int K, void* ws,
+                                size_t ws_bytes, void* stream) {
+  return ptn::zgemm_split(reinterpret_cast<const double2*>(A), lda,
+                          reinterpret_cast<const double2*>(B), ldb, reinterpret_cast<double2*>(C),
+                          ldc, M, N, K, ws, ws_bytes, ptn::as_stream(stream));
+}
+
+int ptn_tc_error(void) {
+  extern int tc_gemm_error_and_reset_c(void);
+  return tc_gemm_error_and_reset_c();
+}
+
+}  // extern "C"

@@ -41,7 +41,7 @@ constexpr int STAGE_BYTES = A_TILE + B_TILE;
 constexpr int THREADS = 192;
 constexpr int TMEM_COLS = 256;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
-constexpr long WAIT_LIMIT = 1L << 24;
+constexpr long WAIT_LIMIT = 1L << 22;
 // kind::f16 instruction descriptor: FP32 accumulate (bit 4), A and B BF16
 // (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
@@ -172,6 +172,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   if (warp == 1) {
+    __syncwarp();
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tslot)),
                  "r"(TMEM_COLS)
@@ -237,12 +238,13 @@ __global__ void __launch_bounds__(THREADS, 1)
     const bool have = ok && (it1 > it0) && !*(volatile int*)abort_flag;
     for (int c0 = 0; c0 < BN; c0 += 16) {
       uint32_t v[16];
+      __syncwarp();
       tmem_ld16(tmem + ((uint32_t)(32 * g) << 16) + (uint32_t)c0, v);
-      if (row >= p.M) continue;
+      if (row < p.M) {
 #pragma unroll
       for (int j = 0; j < 16; j += 2) {
         const int col = n0 + c0 + j;
-        if (col >= p.N) continue;
+        if (col >= p.N) break;
         const float re = have ? __uint_as_float(v[j]) : 0.f;
         const float im = have ? __uint_as_float(v[j + 1]) : 0.f;
         if (p.part != nullptr) {
@@ -259,11 +261,13 @@ __global__ void __launch_bounds__(THREADS, 1)
           *o = x;
         }
       }
+      }
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 1) {
+    __syncwarp();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
                  "r"(TMEM_COLS)
@@ -473,3 +477,5 @@ int tc_gemm_error_and_reset() {
 }
 
 }  // namespace ptn
+
+extern "C" int tc_gemm_error_and_reset_c(void) { return ptn::tc_gemm_error_and_reset(); }

@@ -1,0 +1,118 @@
+"""Mixed-precision (split-BF16 on tcgen05) form: the tensor-core GEMM and the
+contractions against FP64 / the oracle, and whole sweeps against the FP64 form.
+Tolerances: FP32-level relative error (split-BF16 slices carry ~24 bits, FP32
+accumulation), stated per test."""
+
+import numpy as np
+import pytest
+
+from oracle import ptn_oracle as orc
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(x, y):
+    x, y = np.asarray(x), np.asarray(y)
+    return np.linalg.norm(x - y) / max(np.linalg.norm(y), 1e-300)
+
+
+@pytest.fixture(scope="module")
+def ptg():
+    import pytenet_gb300 as m
+    from pytenet_gb300 import _lib
+    _lib.load()
+    return m
+
+
+def split_gemm(A, B):
+    import torch
+    from pytenet_gb300 import _lib
+    from pytenet_gb300.device import to_dev, to_host, ptr, stream_ptr, empty
+    L = _lib.load()
+    M, K = A.shape
+    N = B.shape[1]
+    dA, dB = to_dev(A), to_dev(B)
+    dC = empty((M, N))
+    wsb = L.ptn_zgemm_split_bf16_workspace_bytes(M, N, K)
+    ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+    _lib.check(L.ptn_zgemm_split_bf16(ptr(dA), K, ptr(dB), N, ptr(dC), N, M, N, K, ptr(ws), wsb,
+                                      stream_ptr()))
+    out = to_host(dC)
+    assert L.ptn_tc_error() == 0
+    return out
+
+
+@pytest.mark.parametrize("mnk", [(1, 1, 1), (7, 5, 3), (128, 128, 32), (300, 257, 100),
+                                 (1024, 1024, 512), (2560, 1024, 512), (512, 512, 5120)])
+def test_split_bf16_gemm(ptg, mnk):
+    M, N, K = mnk
+    rng = np.random.default_rng(M + 3 * N + 7 * K)
+    A = orc.crandn((M, K), rng)
+    B = orc.crandn((K, N), rng)
+    C = split_gemm(A, B)
+    ref = A @ B
+    err = rel(C, ref)
+    # ~24-bit operands, FP32 accumulation over K: relative error ~1e-7 * sqrt-ish(K)
+    assert err < 2e-6, err
+
+
+@pytest.mark.parametrize("dims", [(1, 2, 2, 1, 5), (16, 2, 32, 5, 5), (64, 2, 64, 5, 5),
+                                  (130, 2, 97, 4, 5), (256, 2, 256, 5, 5)])
+def test_mixed_contractions(ptg, dims):
+    Dl, d, Dr, cl, cr = dims
+    rng = np.random.default_rng(11 + sum(dims))
+    a = orc.crandn((Dl, d, Dr), rng)
+    w = rng.normal(size=(cl, d, d, cr))
+    w[np.abs(w) < 0.7] = 0.0
+    l = orc.crandn((Dl, cl, Dl), rng)
+    r = orc.crandn((Dr, cr, Dr), rng)
+    tol = 2e-6
+    assert rel(ptg.apply_local_hamiltonian(a, w, l, r, precision="mixed"),
+               orc.apply_local_hamiltonian(a, w, l, r)) < tol
+    assert rel(ptg.contraction_operator_step_left(a, a, w, l, precision="mixed"),
+               orc.env_step_left(a, a, w, l)) < tol
+    assert rel(ptg.contraction_operator_step_right(a, a, w, r, precision="mixed"),
+               orc.env_step_right(a, a, w, r)) < tol
+    c = orc.crandn((Dl, Dr), rng)
+    lb = orc.crandn((Dl, cr, Dl), rng)
+    assert rel(ptg.apply_local_bond_contraction(c, lb, r, precision="mixed"),
+               orc.apply_local_bond_contraction(c, lb, r)) < tol
+
+
+def test_mixed_tdvp_tracks_fp64(ptg):
+    """L=20, D=32 real time, 3 steps: mixed vs FP64 energy and fidelity."""
+    rng = np.random.default_rng(3)
+    L, D = 20, 32
+    h = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 0.8, -0.1)
+    h.zero_qnumbers()
+    b = [min(2 ** min(i, L - i), D) for i in range(L + 1)]
+    psi = ptg.MPS(h.qsite, [bi * [0] for bi in b], fill="random", rng=rng)
+    psi.orthonormalize(mode="left")
+    p64 = ptg.MPS(psi.qsite, psi.qbonds, fill="postpone")
+    p64.a = [x.copy() for x in psi.a]
+    pmx = ptg.MPS(psi.qsite, psi.qbonds, fill="postpone")
+    pmx.a = [x.copy() for x in psi.a]
+    ptg.tdvp_singlesite(h, p64, 0.05j, 3, numiter_lanczos=8, precision="fp64")
+    ptg.tdvp_singlesite(h, pmx, 0.05j, 3, numiter_lanczos=8, precision="mixed")
+    e64 = orc.mpo_average(p64, h).real
+    emx = orc.mpo_average(pmx, h).real
+    ov = orc.mps_vdot(p64, pmx)
+    infid = 1 - abs(ov) ** 2
+    print("energy rel err", abs(emx - e64) / abs(e64), "infidelity", infid)
+    assert abs(emx - e64) < 1e-6 * max(1.0, abs(e64))
+    assert infid < 1e-8
+
+
+def test_mixed_dmrg_energy(ptg):
+    rng = np.random.default_rng(4)
+    L = 12
+    h = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 1.0, 0.0)
+    psi = ptg.MPS.construct_random(L, h.qsite, 0, max_vdim=24, dtype="complex", rng=rng)
+    p2 = ptg.MPS(psi.qsite, psi.qbonds, fill="postpone")
+    p2.a = [x.copy() for x in psi.a]
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        e64 = ptg.dmrg_singlesite(h, psi, 3, numiter_lanczos=20, precision="fp64")
+        emx = ptg.dmrg_singlesite(h, p2, 3, numiter_lanczos=20, precision="mixed")
+    assert abs(emx[-1] - e64[-1]) < 1e-6 * abs(e64[-1])
