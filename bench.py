@@ -47,6 +47,7 @@ def parse():
     p.add_argument("--m", type=int, default=10)
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--e2e-steps", type=int, default=1)
+    p.add_argument("--acc-steps", type=int, default=2)
     p.add_argument("--cpu-sites", type=int, default=3)
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
@@ -301,7 +302,7 @@ def our_arm(a):
     # ---- accuracy of the mixed form vs the FP64 form (same initial state)
     accuracy = None
     if a.form == "mixed" and not a.no_accuracy and rank == 0:
-        accuracy = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, run)
+        accuracy = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0)
 
     # ---- e2e through the public API with host buffers
     e2e = None
@@ -347,25 +348,29 @@ def our_arm(a):
         dist.destroy_process_group()
 
 
-def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, run_mixed):
-    """Energy / fidelity of the mixed run vs the FP64 run from the same state."""
-    from pytenet_gb300.chain_ops import mpo_average, mps_vdot, mps_norm
-    nsteps = run_mixed.steps_done
-    psi_m = ptg.MPS(ptg.MPS(h.qsite, qb0, fill="postpone").qsite, qb0, fill="postpone")
-    run_mixed.chain.download(psi_m)
-    psi_f = ptg.MPS(h.qsite, qb0, fill="postpone")
-    psi_f.a = [x.copy() for x in psi_host0]
-    rf = ptg.TDVPRun(h, psi_f, numiter_lanczos=a.m, precision="fp64")
-    for _ in range(nsteps):
-        rf.step(0.05j)
-    rf.download()
-    e_m, e_f = mpo_average(psi_m, h).real, mpo_average(psi_f, h).real
-    ov = mps_vdot(psi_f, psi_m)
-    nm, nf = mps_norm(psi_m), mps_norm(psi_f)
-    return {"steps": nsteps, "energy_fp64": e_f, "energy_mixed": e_m,
-            "energy_rel_err": abs(e_m - e_f) / max(abs(e_f), 1e-300),
-            "infidelity": 1.0 - abs(ov) ** 2 / (nm * nm * nf * nf),
-            "norm_drift": abs(nm - nf)}
+def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0):
+    """Energy error, infidelity and norm drift of the mixed form against the FP64
+    form after `--acc-steps` steps from the same initial state."""
+    from pytenet_gb300.chain_ops import mpo_average, mps_vdot
+    out = {}
+    runs = {}
+    for form in ("mixed", "fp64"):
+        p = ptg.MPS(h.qsite, qb0, fill="postpone")
+        p.a = [x.copy() for x in psi_host0]
+        r = ptg.TDVPRun(h, p, numiter_lanczos=a.m, precision=form)
+        for _ in range(a.acc_steps):
+            r.step(0.05j)
+        r.download()
+        runs[form] = p
+    pm, pf = runs["mixed"], runs["fp64"]
+    e_m, e_f = mpo_average(pm, h).real, mpo_average(pf, h).real
+    ov = mps_vdot(pf, pm)
+    nm2, nf2 = mps_vdot(pm, pm).real, mps_vdot(pf, pf).real
+    out = {"steps": a.acc_steps, "energy_fp64": e_f, "energy_mixed": e_m,
+           "energy_rel_err": abs(e_m - e_f) / max(abs(e_f), 1e-300),
+           "infidelity": 1.0 - abs(ov) ** 2 / (nm2 * nf2),
+           "norm_drift": abs(np.sqrt(nm2) - np.sqrt(nf2))}
+    return out
 
 
 def main():
