@@ -61,11 +61,14 @@ typedef struct {
   int32_t maxiter;     /* requested number of iterations */
   int32_t status;      /* PTN_OK, or PTN_NAN if the start vector norm was zero / not finite */
   int32_t breakdowns;  /* cumulative count of early stops since the buffer was zeroed */
-  int32_t reserved;
+  int32_t m_target;    /* learned depth at which the residual is tested (0: fixed depth) */
   double nrm;          /* norm of the start vector */
   double beta_next;    /* norm of the residual left after the final iteration */
   double eval0;        /* lowest Ritz value (eigh mode) */
   double resid;        /* a-posteriori error estimate beta_next * |e_m^T f(T) e_1| * nrm */
+  int32_t early_exits; /* cumulative count of accepted learned depths */
+  int32_t iters_total; /* cumulative count of Lanczos vectors used (operator applies) */
+  float feat[12];      /* features of the current local step (learned depth) */
   double alpha[PTN_KRYLOV_MAXITER];
   double beta[PTN_KRYLOV_MAXITER];
   ptn_c128 coef[PTN_KRYLOV_MAXITER];  /* combination coefficients of the Lanczos vectors */
@@ -180,6 +183,48 @@ size_t ptn_bond_step_workspace_bytes(int Dl, int Dr, int chi, int prec);
 ptn_status ptn_expm_bond(ptn_c128* c, const ptn_c128* l, const ptn_c128* r, int Dl, int Dr,
                          int chi, double dt_re, double dt_im, int numiter, int prec,
                          ptn_c128* V, void* state, void* ws, size_t ws_bytes, void* stream);
+/* Learned Lanczos depth for the fused steps (ptn_expm_site_ex / ptn_expm_bond_ex).
+ * After the first Lanczos iteration a 12-64-64-1 MLP (ptn_mlp_*) predicts the
+ * depth m_target from: site position, log2 bond dimensions, step kind, the
+ * scale |dt| |H v0|, and |dt| alpha_0..3 / beta_0..2 of the previous run at the
+ * same site. At depth m_target the a-posteriori estimate
+ * beta_m |e_m^T exp(dt T_m) e_1| / |v| is evaluated on the device; if it is
+ * <= tol the run ends there, otherwise it continues to the full numiter (the
+ * fixed-depth method). No entry point of the reference corresponds to this. */
+typedef struct {
+  const float* params;   /* MLP parameters on the device, or NULL (fixed depth, features only) */
+  float* history;        /* device [nslots][8]: previous alpha_0..3, beta_0..2, valid flag */
+  int slot;              /* history slot of this local step, e.g. 2*site + kind */
+  int site, nsites, kind;/* kind 0: site step, 1: bond step */
+  double tol;            /* relative residual tolerance of the early exit */
+  double* log;           /* device training-record buffer [capacity][PTN_DEPTH_RECORD], or NULL */
+  int* log_count;        /* device record counter */
+  int log_capacity;
+} ptn_depth_ctx;
+#define PTN_DEPTH_RECORD 64   /* doubles per record: 12 features, alpha[24], beta[24], nrm, dt re/im, m_used */
+ptn_status ptn_expm_site_ex(ptn_c128* a, const ptn_c128* w, const ptn_c128* l, const ptn_c128* r,
+                            int Dl, int d, int Dr, int chil, int chir, double dt_re, double dt_im,
+                            int numiter, int prec, const ptn_depth_ctx* depth, ptn_c128* V,
+                            void* state, void* ws, size_t ws_bytes, void* stream);
+ptn_status ptn_expm_bond_ex(ptn_c128* c, const ptn_c128* l, const ptn_c128* r, int Dl, int Dr,
+                            int chi, double dt_re, double dt_im, int numiter, int prec,
+                            const ptn_depth_ctx* depth, ptn_c128* V, void* state, void* ws,
+                            size_t ws_bytes, void* stream);
+/* Labels of recorded runs: the smallest depth m <= m_max whose estimate
+ * beta_{m-1} |e_m^T exp(dt T_m) e_1| is <= tol (m_max if none). */
+ptn_status ptn_depth_labels(const double* log, int count, int m_max, double tol, int* labels,
+                            void* stream);
+
+/* MLP (12 -> 64 -> 64 -> 1, FP32, GELU) for the learned depth: forward pass,
+ * mean-squared-loss gradient (deterministic batch reduction) and Adam update. */
+int ptn_mlp_param_count(void);
+size_t ptn_mlp_workspace_bytes(int batch);
+ptn_status ptn_mlp_forward(const float* params, const float* X, int batch, float* Y, void* stream);
+ptn_status ptn_mlp_grad(const float* params, const float* X, const float* T, int batch,
+                        float* grad, float* loss, void* ws, size_t ws_bytes, void* stream);
+ptn_status ptn_mlp_adam(float* params, const float* grad, float* m, float* v, float lr,
+                        float beta1, float beta2, float eps, int step, void* stream);
+
 /* a9 + a11: a <- lowest Ritz vector of H_eff (pytenet/dmrg.py:181-189); the Ritz
  * value is left in state->eval0. */
 ptn_status ptn_eigh_site(ptn_c128* a, const ptn_c128* w, const ptn_c128* l, const ptn_c128* r,

@@ -45,12 +45,23 @@ def cval(z):
     return c128(z.real, z.imag)
 
 
+class DepthCtx(C.Structure):
+    """Mirror of ptn_depth_ctx."""
+    _fields_ = [("params", C.c_void_p), ("history", C.c_void_p), ("slot", C.c_int),
+                ("site", C.c_int), ("nsites", C.c_int), ("kind", C.c_int), ("tol", C.c_double),
+                ("log", C.c_void_p), ("log_count", C.c_void_p), ("log_capacity", C.c_int)]
+
+
+DEPTH_RECORD = 64
+
+
 class KrylovState(C.Structure):
     """Mirror of ptn_krylov_state."""
     _fields_ = [("m_used", C.c_int32), ("stopped", C.c_int32), ("maxiter", C.c_int32),
-                ("status", C.c_int32), ("breakdowns", C.c_int32), ("reserved", C.c_int32),
+                ("status", C.c_int32), ("breakdowns", C.c_int32), ("m_target", C.c_int32),
                 ("nrm", C.c_double), ("beta_next", C.c_double), ("eval0", C.c_double),
-                ("resid", C.c_double), ("alpha", C.c_double * KRYLOV_MAXITER),
+                ("resid", C.c_double), ("early_exits", C.c_int32), ("iters_total", C.c_int32),
+                ("feat", C.c_float * 12), ("alpha", C.c_double * KRYLOV_MAXITER),
                 ("beta", C.c_double * KRYLOV_MAXITER), ("coef", c128 * KRYLOV_MAXITER)]
 
 
@@ -96,6 +107,14 @@ _SIGS = {
     "ptn_bond_step_workspace_bytes": (S, [I, I, I, I]),
     "ptn_expm_bond": (I, [P, P, P, I, I, I, D, D, I, I, P, P, P, S, P]),
     "ptn_eigh_site": (I, [P, P, P, P, I, I, I, I, I, I, I, P, P, P, S, P]),
+    "ptn_expm_site_ex": (I, [P, P, P, P, I, I, I, I, I, D, D, I, I, P, P, P, P, S, P]),
+    "ptn_expm_bond_ex": (I, [P, P, P, I, I, I, D, D, I, I, P, P, P, P, S, P]),
+    "ptn_depth_labels": (I, [P, I, I, D, P, P]),
+    "ptn_mlp_param_count": (I, []),
+    "ptn_mlp_workspace_bytes": (S, [I]),
+    "ptn_mlp_forward": (I, [P, P, I, P, P]),
+    "ptn_mlp_grad": (I, [P, P, P, I, P, P, P, S, P]),
+    "ptn_mlp_adam": (I, [P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, I, P]),
     "ptn_qr_workspace_bytes": (S, [I, I]),
     "ptn_qr": (I, [P, I, I, P, L, P, L, P, S, P]),
     "ptn_gather": (I, [P, P, P, I, I, P, P]),

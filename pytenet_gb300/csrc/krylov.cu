@@ -20,6 +20,7 @@
 // expm_krylov (krylov.py:122-136) and eigh_krylov (krylov.py:110-119) then reduce
 // to coefficients c_k and one combination pass out = sum_k c_k V[k].
 #include "ptn_common.cuh"
+#include "mlp_common.cuh"
 #include <cfloat>
 #include <algorithm>
 
@@ -87,6 +88,7 @@ __global__ void __launch_bounds__(VT) k_start_finish(KState* st, const double2* 
       st->s.beta_next = 0.0;
       st->s.eval0 = 0.0;
       st->s.resid = 0.0;
+      st->s.m_target = 0;
       st->nblocks = nb;
     }
   }
@@ -277,8 +279,131 @@ __global__ void k_tridiag(KState* st, double dt_re, double dt_im, int mode) {
   __syncwarp();
   if (lane == 0) {
     const ptn_c128 cl = st->s.coef[m - 1];
-    st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im);
+    // an accepted learned depth already stored its relative estimate
+    if (st->s.m_target == 0 || st->s.m_used != st->s.m_target)
+      st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im);
+    st->s.iters_total += m;
   }
+}
+
+// ------------------------------------------------------------------ learned depth
+typedef ptn_depth_ctx DepthArgs;
+
+// c_{m-1} of nrm * U exp(dt Lambda) U^T e_1 for the leading m x m block (all lanes
+// get the value); alpha / beta from the given arrays
+__device__ double2 last_coef(const double* alpha, const double* beta, int m, double nrm,
+                             double dt_re, double dt_im) {
+  const int lane = threadIdx.x & 31;
+  double d[PTN_KRYLOV_MAXITER], e[PTN_KRYLOV_MAXITER], z[PTN_KRYLOV_MAXITER];
+  for (int i = 0; i < m; ++i) {
+    d[i] = alpha[i];
+    e[i] = (i < m - 1) ? beta[i] : 0.0;
+  }
+  // lane 0 carries row 0 of U, lane 1 row m-1 (m >= 2), others idle copies
+  const int row = (lane == 1) ? m - 1 : 0;
+  for (int i = 0; i < m; ++i) z[i] = (i == row) ? 1.0 : 0.0;
+  tridiag_ql(d, e, m, z);
+  double cr = 0.0, ci = 0.0;
+  for (int j = 0; j < m; ++j) {
+    const double u0 = __shfl_sync(0xffffffffu, z[j], 0);
+    const double ul = __shfl_sync(0xffffffffu, z[j], 1);
+    const double a = exp(dt_re * d[j]);
+    double sn, cs;
+    sincos(dt_im * d[j], &sn, &cs);
+    const double f = nrm * u0 * ul * a;
+    cr = fma(f, cs, cr);
+    ci = fma(f, sn, ci);
+  }
+  return make_double2(cr, ci);
+}
+
+// after iteration 0: features of this local step, and the predicted depth
+__global__ void k_predict(KState* st, DepthArgs a, int Dl, int Dr, double dt_abs, int numiter) {
+  __shared__ float x[12];
+  const int lane = threadIdx.x;
+  if (st->s.status != PTN_OK) return;
+  if (lane == 0) {
+    const double a0 = st->s.alpha[0];
+    const double b0 = (st->s.m_used >= 2) ? st->s.beta[0] : st->s.beta_next;
+    const double hv = sqrt(a0 * a0 + b0 * b0);
+    x[0] = (float)a.site / (float)max(1, a.nsites - 1);
+    x[1] = log2f((float)Dl) * 0.1f;
+    x[2] = log2f((float)Dr) * 0.1f;
+    x[3] = (float)a.kind;
+    x[4] = (float)(log10(dt_abs * hv + 1e-300) * 0.25);
+    const float* h = a.history + (long)a.slot * 8;
+    const bool valid = h[7] != 0.f;
+    for (int i = 0; i < 4; ++i) x[5 + i] = valid ? h[i] : (float)(dt_abs * a0);
+    for (int i = 0; i < 3; ++i) x[9 + i] = valid ? h[4 + i] : (float)(dt_abs * b0);
+    for (int i = 0; i < 12; ++i) st->s.feat[i] = x[i];
+  }
+  __syncwarp();
+  if (a.params == nullptr || st->s.stopped) return;
+  const float y = mlpdef::forward_warp(a.params, x);
+  if (lane == 0) {
+    int m = (int)ceilf(y * 20.0f) + 1;   // targets are depth / 20; one step of margin
+    m = max(m, 2);
+    st->s.m_target = (m >= numiter) ? 0 : m;
+  }
+}
+
+// after step j: at the learned depth, accept it if the residual estimate is small
+__global__ void k_depth_check(KState* st, int j, double dt_re, double dt_im, double tol) {
+  if (st->s.stopped || st->s.m_target != j + 1) return;
+  const int m = j + 1;
+  const double nrm = st->s.nrm;
+  const double2 c = last_coef(st->s.alpha, st->s.beta, m, nrm, dt_re, dt_im);
+  const double est = st->s.beta[j] * sqrt(c.x * c.x + c.y * c.y) / nrm;
+  if (threadIdx.x == 0) {
+    if (est <= tol) {
+      st->s.m_used = m;
+      st->s.stopped = 1;
+      st->s.early_exits += 1;
+      st->s.resid = est;
+    } else {
+      st->s.m_target = 0;   // fall back to the full depth
+    }
+  }
+}
+
+// after the coefficients: history of this slot and, optionally, a training record
+__global__ void k_record(KState* st, DepthArgs a, double dt_re, double dt_im) {
+  if (threadIdx.x != 0 || st->s.status != PTN_OK) return;
+  const int m = st->s.m_used;
+  const double dta = sqrt(dt_re * dt_re + dt_im * dt_im);
+  float* h = a.history + (long)a.slot * 8;
+  for (int i = 0; i < 4; ++i) h[i] = (i < m) ? (float)(dta * st->s.alpha[i]) : 0.f;
+  for (int i = 0; i < 3; ++i) h[4 + i] = (i < m - 1) ? (float)(dta * st->s.beta[i]) : 0.f;
+  h[7] = 1.f;
+  if (a.log == nullptr) return;
+  const int idx = atomicAdd(a.log_count, 1);
+  if (idx >= a.log_capacity) return;
+  double* r = a.log + (long)idx * PTN_DEPTH_RECORD;
+  for (int i = 0; i < 12; ++i) r[i] = st->s.feat[i];
+  for (int i = 0; i < 24; ++i) {
+    r[12 + i] = (i < m) ? st->s.alpha[i] : 0.0;
+    r[36 + i] = (i < m - 1) ? st->s.beta[i] : ((i == m - 1) ? st->s.beta_next : 0.0);
+  }
+  r[60] = st->s.nrm;
+  r[61] = dt_re;
+  r[62] = dt_im;
+  r[63] = m;
+}
+
+// labels: smallest depth whose residual estimate meets tol (one warp per record)
+__global__ void k_labels(const double* log, int count, int m_max, double tol, int* labels) {
+  const int rec = blockIdx.x;
+  if (rec >= count) return;
+  const double* r = log + (long)rec * PTN_DEPTH_RECORD;
+  const int mu = min((int)r[63], min(m_max, 24));
+  const double nrm = r[60];
+  int label = m_max;
+  for (int m = 1; m <= mu; ++m) {
+    const double2 c = last_coef(r + 12, r + 36, m, nrm, r[61], r[62]);
+    const double est = r[36 + m - 1] * sqrt(c.x * c.x + c.y * c.y) / nrm;
+    if (est <= tol) { label = m; break; }
+  }
+  if (threadIdx.x == 0) labels[rec] = label;
 }
 
 // Full eigen-decomposition of the tridiagonal matrix, eigenvalues ascending as
@@ -335,6 +460,30 @@ int vec_blocks(long n) {
 }
 
 }  // namespace
+
+ptn_status depth_predict(void* state, const void* args, int Dl, int Dr, double dt_abs, int numiter,
+                         cudaStream_t st) {
+  k_predict<<<1, 32, 0, st>>>(static_cast<KState*>(state), *static_cast<const DepthArgs*>(args), Dl,
+                              Dr, dt_abs, numiter);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
+}
+
+ptn_status depth_check(void* state, int j, double dt_re, double dt_im, double tol, cudaStream_t st) {
+  k_depth_check<<<1, 32, 0, st>>>(static_cast<KState*>(state), j, dt_re, dt_im, tol);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
+}
+
+ptn_status depth_record(void* state, const void* args, double dt_re, double dt_im, cudaStream_t st) {
+  k_record<<<1, 32, 0, st>>>(static_cast<KState*>(state), *static_cast<const DepthArgs*>(args), dt_re,
+                             dt_im);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
+}
 
 size_t krylov_state_bytes() { return (sizeof(KState) + 255) & ~size_t(255); }
 const int32_t* krylov_stop_flag(const void* state) {
@@ -445,6 +594,16 @@ ptn_status ptn_krylov_expm_coef(void* state, double dt_re, double dt_im, void* s
 
 ptn_status ptn_krylov_eigh_coef(void* state, void* stream) {
   return krylov_coef(state, 0.0, 0.0, 1, as_stream(stream));
+}
+
+ptn_status ptn_depth_labels(const double* log, int count, int m_max, double tol, int* labels,
+                            void* stream) {
+  PTN_CHECK_ARG(m_max >= 1 && m_max <= 24, "depth labels: m_max must be in [1, 24]");
+  if (count <= 0) return PTN_OK;
+  k_labels<<<count, 32, 0, as_stream(stream)>>>(log, count, m_max, tol, labels);
+  PTN_LAUNCH_CHECK();
+  note_launches(1);
+  return PTN_OK;
 }
 
 ptn_status ptn_krylov_tridiag_eig(const void* state, double* evals, double* evecs, void* stream) {

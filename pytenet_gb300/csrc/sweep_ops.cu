@@ -18,6 +18,9 @@ ptn_status krylov_step(void*, double2*, long, int, cudaStream_t);
 ptn_status krylov_last(void*, const double2*, const double2*, long, int, bool, cudaStream_t);
 ptn_status krylov_coef(void*, double, double, int, cudaStream_t);
 ptn_status krylov_combine(const void*, const double2*, long, double2*, cudaStream_t);
+ptn_status depth_predict(void*, const void*, int, int, double, int, cudaStream_t);
+ptn_status depth_check(void*, int, double, double, double, cudaStream_t);
+ptn_status depth_record(void*, const void*, double, double, cudaStream_t);
 
 size_t heff_workspace_bytes_f64(int Dl, int d, int Dr, int chil, int chir);
 size_t bond_workspace_bytes_f64(int Dl, int Dr, int chi);
@@ -68,21 +71,30 @@ struct LocalOp {
 
 // mode 0: out = expm(dt H) x; mode 1: out = lowest Ritz vector
 ptn_status krylov_run(const LocalOp& op, double2* x, double dt_re, double dt_im, int numiter,
-                      int mode, double2* V, void* state, cudaStream_t st) {
+                      int mode, double2* V, void* state, cudaStream_t st,
+                      const ptn_depth_ctx* depth = nullptr) {
   PTN_CHECK_ARG(numiter >= 1 && numiter < PTN_KRYLOV_MAXITER, "numiter must be in [1, %d)",
                 PTN_KRYLOV_MAXITER);
   const long n = op.n();
   const int* skip = krylov_stop_flag(state);
   PTN_TRY(op.prepare(st));
   PTN_TRY(krylov_start(state, x, V, n, numiter, st));
+  const double dt_abs = sqrt(dt_re * dt_re + dt_im * dt_im);
   for (int j = 0; j + 1 < numiter; ++j) {
     PTN_TRY(op.apply(V + (long)j * n, V + (long)(j + 1) * n, skip, st));
     PTN_TRY(krylov_step(state, V, n, j, st));
+    if (depth != nullptr) {
+      if (j == 0)
+        PTN_TRY(depth_predict(state, depth, op.Dl, op.Dr, dt_abs, numiter, st));
+      if (depth->params != nullptr && j >= 1)
+        PTN_TRY(depth_check(state, j, dt_re, dt_im, depth->tol, st));
+    }
   }
   double2* w = V + (long)numiter * n;
   PTN_TRY(op.apply(V + (long)(numiter - 1) * n, w, skip, st));
   PTN_TRY(krylov_last(state, V, w, n, numiter - 1, true, st));
   PTN_TRY(krylov_coef(state, dt_re, dt_im, mode, st));
+  if (depth != nullptr) PTN_TRY(depth_record(state, depth, dt_re, dt_im, st));
   PTN_TRY(krylov_combine(state, V, n, x, st));
   return PTN_OK;
 }
@@ -124,6 +136,31 @@ ptn_status ptn_expm_bond(ptn_c128* c, const ptn_c128* l, const ptn_c128* r, int 
              reinterpret_cast<const double2*>(r), ws, ws_bytes};
   return krylov_run(op, reinterpret_cast<double2*>(c), dt_re, dt_im, numiter, 0,
                     reinterpret_cast<double2*>(V), state, as_stream(stream));
+}
+
+ptn_status ptn_expm_site_ex(ptn_c128* a, const ptn_c128* w, const ptn_c128* l, const ptn_c128* r,
+                            int Dl, int d, int Dr, int chil, int chir, double dt_re, double dt_im,
+                            int numiter, int prec, const ptn_depth_ctx* depth, ptn_c128* V,
+                            void* state, void* ws, size_t ws_bytes, void* stream) {
+  PTN_CHECK_ARG(Dl > 0 && d > 0 && Dr > 0 && chil > 0 && chir > 0, "expm_site: bad dims");
+  PTN_CHECK_ARG(depth == nullptr || depth->history != nullptr, "expm_site: depth context needs a history buffer");
+  LocalOp op{true, Dl, d, Dr, chil, chir, prec, reinterpret_cast<const double2*>(w),
+             reinterpret_cast<const double2*>(l), reinterpret_cast<const double2*>(r), ws,
+             ws_bytes};
+  return krylov_run(op, reinterpret_cast<double2*>(a), dt_re, dt_im, numiter, 0,
+                    reinterpret_cast<double2*>(V), state, as_stream(stream), depth);
+}
+
+ptn_status ptn_expm_bond_ex(ptn_c128* c, const ptn_c128* l, const ptn_c128* r, int Dl, int Dr,
+                            int chi, double dt_re, double dt_im, int numiter, int prec,
+                            const ptn_depth_ctx* depth, ptn_c128* V, void* state, void* ws,
+                            size_t ws_bytes, void* stream) {
+  PTN_CHECK_ARG(Dl > 0 && Dr > 0 && chi > 0, "expm_bond: bad dims");
+  PTN_CHECK_ARG(depth == nullptr || depth->history != nullptr, "expm_bond: depth context needs a history buffer");
+  LocalOp op{false, Dl, 1, Dr, chi, chi, prec, nullptr, reinterpret_cast<const double2*>(l),
+             reinterpret_cast<const double2*>(r), ws, ws_bytes};
+  return krylov_run(op, reinterpret_cast<double2*>(c), dt_re, dt_im, numiter, 0,
+                    reinterpret_cast<double2*>(V), state, as_stream(stream), depth);
 }
 
 ptn_status ptn_eigh_site(ptn_c128* a, const ptn_c128* w, const ptn_c128* l, const ptn_c128* r,
