@@ -100,6 +100,23 @@ ptn_status ptn_heff_apply(const ptn_c128* a, const ptn_c128* w, const ptn_c128* 
                           int chil, int chir, int prec, void* ws, size_t ws_bytes,
                           void* stream);
 
+/* H_eff . a exactly as ptn_heff_apply with prec = PTN_PREC_FP64, but without a
+ * workspace argument, for callers that cannot allocate device memory (an FFI host
+ * without a CUDA allocator, a process whose device memory belongs to another
+ * framework's pool, code running where allocation is forbidden). No counterpart
+ * in the reference: it is an addition of this library.
+ * The intermediates live in one file-scope device array of PTN_HEFF_NOALLOC_BYTES
+ * that every GPU loading the library holds until the process exits; sizes with
+ * 2 * Dl * max(d*chir, chil*d) * Dr * 16 bytes above it are rejected with
+ * PTN_BAD_SHAPE. All calls share the array: calls that overlap on the GPU race.
+ * The first call on a device looks the array up (cudaGetSymbolAddress with that
+ * device current); make it before any stream capture. It allocates nothing. */
+#define PTN_HEFF_NOALLOC_BYTES (32u << 20)
+size_t ptn_heff_noalloc_capacity_bytes(void);
+ptn_status ptn_heff_apply_noalloc(const ptn_c128* a, const ptn_c128* w, const ptn_c128* l,
+                                  const ptn_c128* r, ptn_c128* out, int Dl, int d, int Dr,
+                                  int chil, int chir, void* stream);
+
 /* a2: out = zero-site H_eff . c, out[l2, r2] = sum L[l0,w,l2] c[l0,r0] R[r0,w,r2].
  * Replaces apply_local_bond_contraction, pytenet/chain_ops.py:282-317. */
 size_t ptn_bond_workspace_bytes(int Dl, int Dr, int chi, int prec);

@@ -82,6 +82,8 @@ _SIGS = {
     "ptn_prof_read": (I, [I, C.POINTER(D), C.POINTER(D), C.POINTER(D), C.POINTER(L)]),
     "ptn_heff_workspace_bytes": (S, [I, I, I, I, I, I]),
     "ptn_heff_apply": (I, [P, P, P, P, P, I, I, I, I, I, I, P, S, P]),
+    "ptn_heff_noalloc_capacity_bytes": (S, []),
+    "ptn_heff_apply_noalloc": (I, [P, P, P, P, P, I, I, I, I, I, P]),
     "ptn_bond_workspace_bytes": (S, [I, I, I, I]),
     "ptn_bond_apply": (I, [P, P, P, P, I, I, I, I, P, S, P]),
     "ptn_env_workspace_bytes": (S, [I, I, I, I, I, I]),
