@@ -89,6 +89,15 @@ ptn_status mpo_stage(const double2* in, double2* out, const double2* w, long ldq
   return PTN_OK;
 }
 
+}  // namespace
+
+ptn_status mpo_stage_f64(const double2* in, double2* out, const double2* w, long ldq, long ldp, int X,
+                         int P, int Q, int Y, const int* skip, cudaStream_t st) {
+  return mpo_stage(in, out, w, ldq, ldp, X, P, Q, Y, skip, st);
+}
+
+namespace {
+
 inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 GemmArgs gemm_args(char oa, char ob, int M, int N, int K, const double2* A, long lda,

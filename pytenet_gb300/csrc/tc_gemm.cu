@@ -1,29 +1,37 @@
-// Split-BF16 complex GEMM on the 5th-generation tensor cores (tcgen05, sm_103a).
+// Split-BF16 complex GEMM on the 5th-generation tensor cores (tcgen05, sm_103a),
+// with FP64-class accuracy from exact fixed-point digit products.
 //
-// A complex product C = op(A) op(B) is computed as one real GEMM on BF16 slices
-// with FP32 accumulation in tensor memory:
-//   - every FP64 value x is split into three BF16 slices x = x0 + x1 + x2 (8
-//     significant bits each, ~24 bits together);
+// A complex product C = op(A) op(B) is computed as one real GEMM:
 //   - the "plain" operand A is the row-major complex matrix read as real
 //     (M x 2K: re/im interleaved along K), the "embedded" operand B holds each
 //     complex entry z as the 2x2 real block [[Re z, -Im z], [Im z, Re z]]
 //     (2N x 2K, K-major), so that the real product (M x 2N) is the complex
 //     product with re/im interleaved -- i.e. the complex128 output layout;
-//   - the slice products sum_{i+j<=2} A_i B_j (six pairs, smallest first) are
-//     accumulated in one FP32 tensor-memory accumulator; long K is split across
-//     CTAs whose FP32 partials are summed in FP64.
+//   - every operand row r is scaled by its own power of two 2^-e[r] (|x| < 2^e[r]
+//     over the row) and cut into four signed 8-bit integer digits held exactly in
+//     BF16: x = 2^(e[r]-7) * sum_i 2^(-8 i) d_i, |d_i| <= 128 (Ozaki, Ogita, Oishi
+//     and Rump's error-free splitting, in fixed point per row);
+//   - a digit product is an integer of at most 14 bits, so the products of one
+//     level s = i + j (pairs with s <= 3, ten in all) add up exactly in an FP32
+//     accumulator as long as the partial sums stay below 2^24; each level has its
+//     own accumulator in tensor memory (4 levels x 128 columns = all 512 columns);
+//   - the epilogue combines the levels in FP64, sum_s 2^(-8 s) acc_s, and applies
+//     the row and column scales 2^(eA[m] + eB[n] - 14). Split-K partials are FP64.
+// What remains is the truncation of the fourth digit, ~2^-31 of the row maxima.
 //
-// Kernel: one 128 x 256 output tile per CTA (UMMA M=128, N=256, K=16), BK=64
-// (one 128-byte swizzle atom of BF16), 4-stage TMA -> shared memory pipeline with
-// full/empty mbarriers. Warp 0 lane 0 issues TMA, warp 1 lane 0 issues
-// tcgen05.mma and tcgen05.commit, warps 2..5 read the accumulator back with
-// tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..) and write FP64 complex results
-// (or FP32 split-K partials). Every mbarrier wait is bounded: on expiry the
-// kernel records an error code, stops issuing work and still frees its TMEM.
+// Kernel: one 128 x 128 output tile per CTA (UMMA M=128, N=128, K=16), BK=64
+// (one 128-byte swizzle atom of BF16), 6-stage TMA -> shared memory pipeline with
+// full/empty mbarriers over (k block, digit pair) steps. Warp 0 lane 0 issues TMA,
+// warp 1 lane 0 issues tcgen05.mma and tcgen05.commit, warps 2..5 read the four
+// accumulators back with tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..) and write
+// FP64 complex results (or FP64 split-K partials). Every mbarrier wait is bounded:
+// on expiry the kernel records an error code, stops issuing work, lets its copies
+// in flight land and still frees its TMEM.
 #include "ptn_common.cuh"
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <algorithm>
+#include <climits>
 #include <mutex>
 #include <vector>
 
@@ -33,33 +41,45 @@ void note_launches(int n);
 
 namespace {
 
-constexpr int BM = 128, BN = 256, BK = 64;
-constexpr int STAGES = 4;
+constexpr int BM = 128, BN = 128, BK = 64;
+constexpr int STAGES = 6;
+constexpr int NDIGIT = 4;                 // digits per operand value
+constexpr int NPAIR = 10;                 // digit pairs (i, j) with i + j <= 3
+constexpr int NLEVEL = 4;
+// operand rows without a non-zero entry carry an exponent below this (the digit
+// converter fills the exponent arrays with 0x80 bytes before its max pass)
+constexpr int EXP_NONE = -2000;
 constexpr int A_TILE = BM * BK * 2;
 constexpr int B_TILE = BN * BK * 2;
 constexpr int STAGE_BYTES = A_TILE + B_TILE;
 constexpr int THREADS = 192;
-constexpr int TMEM_COLS = 256;
+constexpr int TMEM_COLS = NLEVEL * BN;   // 512: one accumulator per level
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long WAIT_LIMIT = 1L << 22;
 // kind::f16 instruction descriptor: FP32 accumulate (bit 4), A and B BF16
 // (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
+static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
 
 struct TcArgs {
   int M, N;            // output rows, real output columns (2 x complex columns)
-  int nkb;             // K blocks (of BK) per slice pair
-  int npairs;
-  int pa[8], pb[8];    // slice indices per pair
-  int it_per_split, splits;
+  int nkb;             // K blocks (of BK)
+  int kb_per_split, splits;
+  const int* ea;       // row exponents of A (M), below EXP_NONE for an all-zero row
+  const int* eb;       // exponents of B per complex column (N / 2)
   double2* out;        // complex output element (m, c) at out[m * ldm + c * ldn]
   long ldm, ldn;
   int accumulate;      // out += result instead of out = result
-  float* part;         // split-K partials [splits][M][N], or null
+  double* part;        // split-K partials [splits][M][N], or null
   int* err;
   const int* skip;
 };
+
+// digit pairs, grouped by level; the first pair of each level starts its accumulator
+__constant__ int c_pair_a[NPAIR] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
+__constant__ int c_pair_b[NPAIR] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
+__constant__ int c_pair_l[NPAIR] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -157,9 +177,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
   const int split = blockIdx.z;
-  const int total = p.npairs * p.nkb;
-  const int it0 = split * p.it_per_split;
-  const int it1 = min(total, it0 + p.it_per_split);
+  const int kb0 = split * p.kb_per_split;
+  const int kb1 = min(p.nkb, kb0 + p.kb_per_split);
+  // steps: k block outer, digit pair inner
+  const int it0 = kb0 * NPAIR, it1 = kb1 * NPAIR;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -196,10 +217,10 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       if (*(volatile int*)abort_flag) break;
-      const int pr = it / p.nkb, kb = it % p.nkb;
+      const int kb = it / NPAIR, pr = it % NPAIR;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_3d(sA + s * A_TILE, &tmA, kb * BK, m0, p.pa[pr], &full[s]);
-      tma_load_3d(sB + s * B_TILE, &tmB, kb * BK, n0, p.pb[pr], &full[s]);
+      tma_load_3d(sA + s * A_TILE, &tmA, kb * BK, m0, c_pair_a[pr], &full[s]);
+      tma_load_3d(sB + s * B_TILE, &tmB, kb * BK, n0, c_pair_b[pr], &full[s]);
       ++issued;
     }
     if (*(volatile int*)abort_flag) {
@@ -219,48 +240,73 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int pr = it % NPAIR;
+      const uint32_t acc_col = (uint32_t)(c_pair_l[pr] * BN);
+      // the first k block of this split starts each level's accumulator
+      const bool first_of_level = (it / NPAIR == kb0) &&
+                                  (pr == 0 || c_pair_l[pr] != c_pair_l[pr - 1]);
       const uint32_t a0 = smem_u32(sA + s * A_TILE), b0 = smem_u32(sB + s * B_TILE);
 #pragma unroll
       for (int k = 0; k < BK / 16; ++k)
-        umma(tmem, sdesc(a0 + k * 32), sdesc(b0 + k * 32), (i > 0 || k > 0) ? 1u : 0u);
+        umma(tmem + acc_col, sdesc(a0 + k * 32), sdesc(b0 + k * 32),
+             (first_of_level && k == 0) ? 0u : 1u);
       umma_commit(&empty[s]);
       ++issued;
     }
     if (issued > 0) umma_commit(tfull);
     else mbar_arrive(tfull);
   } else if (warp >= 2) {
-    // ---------------- epilogue: TMEM -> registers -> global
+    // ---------------- epilogue: 4 level accumulators -> FP64 -> global
     const bool ok = mbar_wait(tfull, 0);
     if (!ok) atomicExch(p.err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const int g = warp & 3;
     const int row = m0 + 32 * g + lane;
     const bool have = ok && (it1 > it0) && !*(volatile int*)abort_flag;
+    const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
+    const uint32_t tl = tmem + ((uint32_t)(32 * g) << 16);
     for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t v[16];
+      uint32_t v0[16], v1[16], v2[16], v3[16];
       __syncwarp();
-      tmem_ld16(tmem + ((uint32_t)(32 * g) << 16) + (uint32_t)c0, v);
+      tmem_ld16(tl + (uint32_t)c0, v0);
+      tmem_ld16(tl + (uint32_t)(BN + c0), v1);
+      tmem_ld16(tl + (uint32_t)(2 * BN + c0), v2);
+      tmem_ld16(tl + (uint32_t)(3 * BN + c0), v3);
       if (row < p.M) {
 #pragma unroll
-      for (int j = 0; j < 16; j += 2) {
-        const int col = n0 + c0 + j;
-        if (col >= p.N) break;
-        const float re = have ? __uint_as_float(v[j]) : 0.f;
-        const float im = have ? __uint_as_float(v[j + 1]) : 0.f;
-        if (p.part != nullptr) {
-          float2* dst = reinterpret_cast<float2*>(p.part + ((long)split * p.M + row) * p.N + col);
-          *dst = make_float2(re, im);
-        } else {
-          double2* o = p.out + (long)row * p.ldm + (long)(col >> 1) * p.ldn;
-          double2 x = make_double2((double)re, (double)im);
-          if (p.accumulate) {
-            const double2 y = *o;
-            x.x += y.x;
-            x.y += y.y;
+        for (int j = 0; j < 16; j += 2) {
+          const int col = n0 + c0 + j;
+          if (col >= p.N) break;
+          double re = 0.0, im = 0.0;
+          const int eb = p.eb[col >> 1];
+          if (have && ea > EXP_NONE && eb > EXP_NONE) {
+            // smallest level first; every FP32 -> FP64 conversion is exact
+            re = (double)__uint_as_float(v3[j]);
+            re = fma(re, 0x1p-8, (double)__uint_as_float(v2[j]));
+            re = fma(re, 0x1p-8, (double)__uint_as_float(v1[j]));
+            re = fma(re, 0x1p-8, (double)__uint_as_float(v0[j]));
+            im = (double)__uint_as_float(v3[j + 1]);
+            im = fma(im, 0x1p-8, (double)__uint_as_float(v2[j + 1]));
+            im = fma(im, 0x1p-8, (double)__uint_as_float(v1[j + 1]));
+            im = fma(im, 0x1p-8, (double)__uint_as_float(v0[j + 1]));
+            const double sc = ldexp(1.0, ea + eb - 14);
+            re *= sc;
+            im *= sc;
           }
-          *o = x;
+          if (p.part != nullptr) {
+            double2* dst = reinterpret_cast<double2*>(p.part + ((long)split * p.M + row) * p.N + col);
+            *dst = make_double2(re, im);
+          } else {
+            double2* o = p.out + (long)row * p.ldm + (long)(col >> 1) * p.ldn;
+            double2 x = make_double2(re, im);
+            if (p.accumulate) {
+              const double2 y = *o;
+              x.x += y.x;
+              x.y += y.y;
+            }
+            *o = x;
+          }
         }
-      }
       }
     }
   }
@@ -275,7 +321,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
-__global__ void splitk_sum_kernel(const float* __restrict__ part, int splits, int M, int N,
+__global__ void splitk_sum_kernel(const double* __restrict__ part, int splits, int M, int N,
                                   double2* __restrict__ out, long ldm, long ldn, int accumulate,
                                   const int* skip) {
   if (skip != nullptr && *skip != 0) return;
@@ -288,9 +334,9 @@ __global__ void splitk_sum_kernel(const float* __restrict__ part, int splits, in
     const int m = (int)(idx % M), c = (int)(idx / M);
     double re = 0.0, im = 0.0;
     for (int s = 0; s < splits; ++s) {
-      const float2 v = *reinterpret_cast<const float2*>(part + ((long)s * M + m) * N + 2 * c);
-      re += (double)v.x;
-      im += (double)v.y;
+      const double2 v = *reinterpret_cast<const double2*>(part + ((long)s * M + m) * N + 2 * c);
+      re += v.x;
+      im += v.y;
     }
     double2* o = out + (long)m * ldm + (long)c * ldn;
     if (accumulate) {
@@ -342,7 +388,7 @@ MapCache& map_cache() {
   return c;
 }
 
-// 3-D map over slices [3][rows][Kp] of BF16, logical extent (K, rows, 3), box (64, box_rows, 1)
+// 3-D map over digit planes [4][rows][Kp] of BF16, logical extent (K, rows, 4), box (64, box_rows, 1)
 bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, long plane,
               int box_rows) {
   MapKey key{ptr, rows, K, Kp, plane, box_rows};
@@ -357,7 +403,7 @@ bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, lon
   }
   EncodeTiledFn fn = encode_fn();
   if (fn == nullptr) return false;
-  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, 3};
+  cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)NDIGIT};
   cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)plane * 2};
   cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
   cuuint32_t estr[3] = {1, 1, 1};
@@ -388,31 +434,34 @@ int* err_flag() {
 
 }  // namespace
 
-// Slice-pair schedule of the split-BF16 product, smallest terms first.
-static const int kPairA[6] = {2, 1, 0, 1, 0, 0};
-static const int kPairB[6] = {0, 1, 2, 0, 1, 0};
+static int choose_splits(int M, int N, int nkb) {
+  const int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  const int target = 2 * num_sms();
+  int splits = 1;
+  if (tiles < target) splits = std::max(1, std::min((target + tiles - 1) / tiles, nkb / 2));
+  // keep each split's exact integer sums short: at most 32 K blocks (2048 reals) per split
+  splits = std::max(splits, (nkb + 31) / 32);
+  return std::min(splits, nkb);
+}
 
 size_t tc_gemm_workspace_bytes(int M, int Ncomplex, int Kcomplex) {
   const int N = 2 * Ncomplex, K = 2 * Kcomplex;
-  const int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
   const int nkb = (K + BK - 1) / BK;
-  const int total = 6 * nkb;
-  int splits = 1;
-  const int target = 2 * num_sms();
-  if (tiles < target) splits = std::max(1, std::min((target + tiles - 1) / tiles, total / 8));
-  return splits > 1 ? (size_t)splits * M * N * sizeof(float) : 0;
+  const int splits = choose_splits(M, N, nkb);
+  return splits > 1 ? (size_t)splits * M * N * sizeof(double) : 0;
 }
 
-// C (M x Nc complex) = A (M x Kc) * B (Kc x Nc) from slice buffers:
-//   Aslices: [3][M][Kp] BF16 (plain), Bslices: [3][2 Nc][Kp] BF16 (embedded), Kp >= 2 Kc, Kp % 8 == 0.
-ptn_status tc_gemm(const void* Aslices, long aplane, const void* Bslices, long bplane, int M,
-                   int Nc, int Kc, long Kp, double2* out, long ldm, long ldn, bool accumulate,
-                   void* ws, size_t ws_bytes, const int* skip, cudaStream_t st) {
+// C (M x Nc complex) = A (M x Kc) * B (Kc x Nc) from digit planes:
+//   Aslices: [4][M][Kp] BF16 (plain) with row exponents ea[M],
+//   Bslices: [4][2 Nc][Kp] BF16 (embedded) with exponents eb[Nc]; Kp >= 2 Kc, Kp % 8 == 0.
+ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* Bslices, long bplane,
+                   const int* eb, int M, int Nc, int Kc, long Kp, double2* out, long ldm, long ldn,
+                   bool accumulate, void* ws, size_t ws_bytes, const int* skip, cudaStream_t st) {
   const int N = 2 * Nc, K = 2 * Kc;
   PTN_CHECK_ARG(M > 0 && Nc > 0 && Kc > 0 && Kp >= K && Kp % 8 == 0, "tc_gemm: bad sizes");
   PTN_CHECK_ARG(reinterpret_cast<uintptr_t>(Aslices) % 16 == 0 &&
                     reinterpret_cast<uintptr_t>(Bslices) % 16 == 0,
-                "tc_gemm: slice buffers must be 16-byte aligned");
+                "tc_gemm: digit buffers must be 16-byte aligned");
   CUtensorMap ma, mb;
   if (!make_map(&ma, Aslices, M, K, Kp, aplane, BM) || !make_map(&mb, Bslices, N, K, Kp, bplane, BN)) {
     set_error("tc_gemm: cuTensorMapEncodeTiled failed");
@@ -428,28 +477,28 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const void* Bslices, long b
   a.M = M;
   a.N = N;
   a.nkb = (K + BK - 1) / BK;
-  a.npairs = 6;
-  for (int i = 0; i < 6; ++i) { a.pa[i] = kPairA[i]; a.pb[i] = kPairB[i]; }
-  const int total = a.npairs * a.nkb;
   const int gx = (N + BN - 1) / BN, gy = (M + BM - 1) / BM;
-  int splits = 1;
-  const int target = 2 * num_sms();
-  if (gx * gy < target) splits = std::max(1, std::min((target + gx * gy - 1) / (gx * gy), total / 8));
-  while (splits > 1 && (size_t)splits * M * N * sizeof(float) > ws_bytes) --splits;
-  a.it_per_split = (total + splits - 1) / splits;
-  splits = (total + a.it_per_split - 1) / a.it_per_split;   // no empty split
+  int splits = choose_splits(M, N, a.nkb);
+  if (splits > 1 && (size_t)splits * M * N * sizeof(double) > ws_bytes) {
+    set_error("tc_gemm: workspace too small for %d K splits", splits);
+    return PTN_BAD_SHAPE;
+  }
+  a.kb_per_split = (a.nkb + splits - 1) / splits;
+  splits = (a.nkb + a.kb_per_split - 1) / a.kb_per_split;   // no empty split
   a.splits = splits;
+  a.ea = ea;
+  a.eb = eb;
   a.out = out;
   a.ldm = ldm;
   a.ldn = ldn;
   a.accumulate = accumulate ? 1 : 0;
-  a.part = splits > 1 ? static_cast<float*>(ws) : nullptr;
+  a.part = splits > 1 ? static_cast<double*>(ws) : nullptr;
   a.err = err_flag();
   a.skip = skip;
   PTN_CHECK_ARG(a.err != nullptr, "tc_gemm: error flag lookup failed");
   PTN_CHECK_ARG(gy <= 65535 && splits <= 65535, "tc_gemm: grid too large");
   const int prof = prof_begin(st, PROF_TC_GEMM, 8.0 * M * (double)Nc * Kc,
-                              2.0 * 3 * ((double)M * Kp + (double)N * Kp) + 16.0 * M * Nc);
+                              2.0 * NDIGIT * ((double)M * Kp + (double)N * Kp) + 16.0 * M * Nc);
   tc_gemm_kernel<<<dim3(gx, gy, splits), THREADS, SMEM_BYTES, st>>>(ma, mb, a);
   PTN_LAUNCH_CHECK();
   note_launches(1);
