@@ -9,14 +9,21 @@
 // README workload clamps bonds) the completion of Q determines the later sweep.
 //
 // Structure (blocked, compact WY):  for each panel of NB columns
-//   panel kernel  : one CTA factors the panel column by column and builds the
-//                   NB x NB triangular factor T with H_1..H_nb = I - V T V^H;
+//   panel kernel  : a cluster of up to 16 CTAs factors the panel column by
+//                   column -- each CTA owns a slice of the rows, the column norm
+//                   and the reflector dot products are reduced across the
+//                   cluster through distributed shared memory (two cluster
+//                   barriers per column) -- and builds the NB x NB triangular
+//                   factor T with H_1..H_nb = I - V T V^H;
 //   block update  : A_trail -= V (T^H (V^H A_trail)), as two grid-wide passes
 //                   (partial V^H A per 64-row tile, then reduce + apply);
 // then Q = H_1 ... H_k [I; 0] is formed backwards with the same block update
 // (using T instead of T^H).
 #include "ptn_common.cuh"
+#include <cooperative_groups.h>
 #include <algorithm>
+
+namespace cg = cooperative_groups;
 
 namespace ptn {
 
@@ -174,30 +181,629 @@ __global__ void __launch_bounds__(PT) qr_panel_kernel(double2* __restrict__ a, l
   if (tid < NB * NB) Tout[tid] = sT[tid / NB][tid % NB];
 }
 
+// Cluster version of the panel factorisation: CTA `rank` of the cluster owns rows
+// [j0 + rank * chunk, j0 + (rank + 1) * chunk). All reductions sum the per-CTA
+// partials in rank order, so every CTA derives identical reflectors.
+constexpr int CPT = 256;   // threads per cluster CTA
+
+__global__ void __launch_bounds__(CPT) qr_panel_cluster_kernel(double2* __restrict__ a, long lda,
+                                                               int m, int j0, int jb,
+                                                               double2* __restrict__ Tout,
+                                                               double2* __restrict__ V, long ldv) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int cs = (int)cluster.num_blocks();
+  const int tid = threadIdx.x;
+  __shared__ double sh[33];
+  __shared__ double2 red[CPT / 32][NB];
+  __shared__ double s_nrm;
+  __shared__ double2 s_alpha;
+  __shared__ double2 s_w[NB];       // this CTA's partial vector (read remotely)
+  __shared__ double2 gath[16][NB];  // all CTAs' partial vectors (cluster size <= 16)
+  __shared__ double2 wv[NB];        // cluster-reduced vector
+  __shared__ double2 taus[NB];
+  __shared__ double2 sT[NB][NB];
+  __shared__ double2 s_scal;
+  __shared__ double s_beta;
+  __shared__ int s_apply;
+
+  const int mp = m - j0;
+  const int chunk = (mp + cs - 1) / cs;
+  const int rb = j0 + rank * chunk;
+  const int re = min(m, rb + chunk);
+
+  for (int jj = 0; jj < jb; ++jj) {
+    const int col = j0 + jj;
+    const int owner = jj / chunk;            // CTA holding row col
+    double acc = 0.0;
+    for (int i = max(rb, col + 1) + tid; i < re; i += CPT) {
+      const double2 v = a[(long)i * lda + col];
+      acc = fma(v.x, v.x, acc);
+      acc = fma(v.y, v.y, acc);
+    }
+    acc = block_sum(acc, sh);
+    if (tid == 0) {
+      s_nrm = acc;
+      if (rank == owner) s_alpha = a[(long)col * lda + col];
+    }
+    cluster.sync();
+    if (tid < 32) {
+      // one remote load per lane, then a fixed-order tree: identical in every CTA
+      double v = (tid < cs) ? *cluster.map_shared_rank(&s_nrm, tid) : 0.0;
+      const double2 alpha_l = (tid == 0) ? *cluster.map_shared_rank(&s_alpha, owner) : c2(0.0, 0.0);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      const double xn2 = v;
+      const double2 alpha = alpha_l;
+      if (tid == 0) {
+      if (xn2 == 0.0 && alpha.y == 0.0) {
+        taus[jj] = c2(0.0, 0.0);
+        s_apply = 0;
+      } else {
+        const double beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        taus[jj] = c2((beta - alpha.x) / beta, -alpha.y / beta);
+        s_scal = crecip(c2(alpha.x - beta, alpha.y));
+        s_beta = beta;
+        s_apply = 1;
+      }
+      }
+    }
+    __syncthreads();
+    const int apply = s_apply;
+    if (apply) {
+      const double2 sc = s_scal;
+      for (int i = max(rb, col + 1) + tid; i < re; i += CPT) {
+        double2* p = a + (long)i * lda + col;
+        *p = cmul(*p, sc);
+      }
+      if (tid == 0 && rank == owner) a[(long)col * lda + col] = c2(s_beta, 0.0);
+    }
+    __syncthreads();
+    const int nrem = j0 + jb - col - 1;
+    // every CTA takes part in the barrier below, also when there is nothing to apply
+    double2 part[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) part[c] = c2(0.0, 0.0);
+    if (apply && nrem > 0) {
+      for (int i = max(rb, col) + tid; i < re; i += CPT) {
+        const double2 v = (i == col) ? c2(1.0, 0.0) : a[(long)i * lda + col];
+        const double2 vc = cconj(v);
+        const double2* row = a + (long)i * lda + col + 1;
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+          if (c < nrem) part[c] = cfma(vc, row[c], part[c]);
+      }
+    }
+    block_reduce_vec(part, NB, red, s_w);
+    cluster.sync();
+    // gather all CTAs' partial vectors with one remote load per thread, then sum in rank order
+    if (tid < cs * NB) gath[tid / NB][tid % NB] = cluster.map_shared_rank(s_w, tid / NB)[tid % NB];
+    __syncthreads();
+    if (tid < NB) {
+      double2 sacc = c2(0.0, 0.0);
+      for (int r = 0; r < cs; ++r) sacc = cadd(sacc, gath[r][tid]);
+      wv[tid] = sacc;
+    }
+    __syncthreads();
+    if (apply && nrem > 0) {
+      const double2 ctau = cconj(taus[jj]);
+      for (int i = max(rb, col) + tid; i < re; i += CPT) {
+        const double2 v = (i == col) ? c2(1.0, 0.0) : a[(long)i * lda + col];
+        const double2 f = cmul(ctau, v);
+        double2* row = a + (long)i * lda + col + 1;
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+          if (c < nrem) row[c] = csub(row[c], cmul(f, wv[c]));
+      }
+    }
+    __syncthreads();
+  }
+
+  // explicit V for the panel columns on this CTA's rows
+  for (int i = rb + tid; i < re; i += CPT) {
+    for (int c = 0; c < jb; ++c) {
+      const int col = j0 + c;
+      V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0)
+                               : (i == col) ? c2(1.0, 0.0) : a[(long)i * lda + col];
+    }
+  }
+  // partial Gram G[p][c] = v_p^H v_c (p < c) over this CTA's rows -> s_G
+  __shared__ double2 s_G[NB][NB];
+  if (tid < NB * NB) s_G[tid / NB][tid % NB] = c2(0.0, 0.0);
+  __syncthreads();
+  for (int c = 1; c < jb; ++c) {
+    double2 pp[NB];
+#pragma unroll
+    for (int p = 0; p < NB; ++p) pp[p] = c2(0.0, 0.0);
+    for (int i = max(rb, j0 + c) + tid; i < re; i += CPT) {
+      const double2 vc = (i == j0 + c) ? c2(1.0, 0.0) : a[(long)i * lda + j0 + c];
+#pragma unroll
+      for (int p = 0; p < NB; ++p)
+        if (p < c) {
+          const double2 vp = (i == j0 + p) ? c2(1.0, 0.0) : a[(long)i * lda + j0 + p];
+          pp[p] = cfma(cconj(vp), vc, pp[p]);
+        }
+    }
+    block_reduce_vec(pp, c, red, wv);
+    if (tid < c) s_G[tid][c] = wv[tid];
+    __syncthreads();
+  }
+  cluster.sync();
+  if (rank == 0) {
+    // sum the Gram partials of all CTAs (rank order), then T as in zlarft
+    if (tid < NB * NB) {
+      const int p = tid / NB, c = tid % NB;
+      double2 g = c2(0.0, 0.0);
+      for (int r = 0; r < cs; ++r) g = cadd(g, cluster.map_shared_rank(&s_G[0][0], r)[p * NB + c]);
+      sT[p][c] = g;   // the summed Gram (upper part)
+    }
+    __syncthreads();
+    // T column by column (zlarft); column c needs only columns < c of T
+    if (tid < NB * NB) s_G[tid / NB][tid % NB] = c2(0.0, 0.0);   // now holds T
+    __syncthreads();
+    for (int c = 0; c < jb; ++c) {
+      if (tid < c) {
+        const int p = tid;
+        double2 acc2 = c2(0.0, 0.0);
+        for (int q = p; q < c; ++q) acc2 = cadd(acc2, cmul(s_G[p][q], sT[q][c]));
+        s_G[p][c] = cmul(c2(-taus[c].x, -taus[c].y), acc2);
+      }
+      if (tid == 0) s_G[c][c] = taus[c];
+      __syncthreads();
+    }
+    if (tid < NB * NB) Tout[tid] = s_G[tid / NB][tid % NB];
+  }
+  cluster.sync();   // no CTA leaves while its shared memory may still be read
+}
+
+// Latency-lean panel factorisation: a cluster of CS CTAs of ONE warp each. CTA
+// `rank` owns rows [j0 + rank*chunk, ...) and keeps them in registers (lane l,
+// slot t holds local row t*32 + l, all NB panel columns). Per column: a shuffle
+// reduction of the norm, one cluster barrier, every lane gathers the CTA partials
+// (DSMEM) and computes the reflector redundantly, the dot products are shuffle-
+// reduced, a second barrier, a gather, the rank-1 update -- no __syncthreads at
+// all, and the dependent FP64 chain per column is kept short (GB300's FP64
+// latency is 64 cycles per add/FMA).
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <int ROWS>
+__global__ void __launch_bounds__(32) qr_panel_warp_kernel(double2* __restrict__ a, long lda, int m,
+                                                           int j0, int jb,
+                                                           double2* __restrict__ Tout,
+                                                           double2* __restrict__ V, long ldv) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int cs = (int)cluster.num_blocks();
+  const int lane = threadIdx.x;
+  __shared__ double s_nrm;
+  __shared__ double2 s_alpha;
+  __shared__ double2 s_w[NB];
+  __shared__ double2 s_G[NB][NB];
+
+  const int mp = m - j0;
+  const int chunk = (mp + cs - 1) / cs;
+  const int rb = j0 + rank * chunk;
+  const int re = min(m, rb + chunk);
+
+  // panel rows in registers
+  double2 x[ROWS][NB];
+#pragma unroll
+  for (int t = 0; t < ROWS; ++t) {
+    const int i = rb + t * 32 + lane;
+#pragma unroll
+    for (int c = 0; c < NB; ++c)
+      x[t][c] = (i < re && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
+  }
+  double2 taus_l[NB];   // every lane keeps all tau (uniform across lanes)
+
+#pragma unroll
+  for (int jj = 0; jj < NB; ++jj) {
+    if (jj < jb) {
+      const int col = j0 + jj;
+      const int owner = jj / chunk;
+      // ---- norm of the sub-diagonal part of column jj
+      double acc = 0.0;
+#pragma unroll
+      for (int t = 0; t < ROWS; ++t) {
+        const int i = rb + t * 32 + lane;
+        if (i > col && i < re) acc = fma(x[t][jj].x, x[t][jj].x, fma(x[t][jj].y, x[t][jj].y, acc));
+      }
+      acc = wsum(acc);
+      if (lane == 0) s_nrm = acc;
+      if (rank == owner) {
+        const int lr = col - rb;
+#pragma unroll
+        for (int t = 0; t < ROWS; ++t)
+          if (lr - t * 32 == lane) s_alpha = x[t][jj];
+      }
+      cluster.sync();
+      double v = (lane < cs) ? *cluster.map_shared_rank(&s_nrm, lane) : 0.0;
+      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
+      const double xn2 = wsum(v);
+      // ---- reflector (zlarfg), computed by every lane
+      double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
+      double beta = 0.0;
+      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
+      if (apply) {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        const double ib = 1.0 / beta;
+        tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
+        scal = crecip(c2(alpha.x - beta, alpha.y));
+      }
+      taus_l[jj] = tau;
+      // ---- scale own rows below the diagonal, set the diagonal
+#pragma unroll
+      for (int t = 0; t < ROWS; ++t) {
+        const int i = rb + t * 32 + lane;
+        if (apply && i > col && i < re) x[t][jj] = cmul(x[t][jj], scal);
+        if (apply && i == col) x[t][jj] = c2(beta, 0.0);
+      }
+      // ---- w_c = v^H a_c for the remaining panel columns (v_col = 1)
+      double2 w[NB];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) w[c] = c2(0.0, 0.0);
+#pragma unroll
+      for (int t = 0; t < ROWS; ++t) {
+        const int i = rb + t * 32 + lane;
+        if (apply && i >= col && i < re) {
+          const double2 vc = (i == col) ? c2(1.0, 0.0) : cconj(x[t][jj]);
+#pragma unroll
+          for (int c = 0; c < NB; ++c)
+            if (c > jj) w[c] = cfma(vc, x[t][c], w[c]);
+        }
+      }
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c > jj) {
+          w[c].x = wsum(w[c].x);
+          w[c].y = wsum(w[c].y);
+        }
+      }
+      if (lane < NB) {
+        double2 mine = c2(0.0, 0.0);
+#pragma unroll
+        for (int c = 0; c < NB; ++c)
+          if (c == lane) mine = w[c];
+        s_w[lane] = mine;
+      }
+      cluster.sync();
+      // ---- gather the CTA partials: lane c sums rank by rank (same order in every CTA)
+      double2 wc = c2(0.0, 0.0);
+      if (lane < NB && lane > jj) {
+        double2 vals[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+          vals[r] = (r < cs) ? cluster.map_shared_rank(s_w, r)[lane] : c2(0.0, 0.0);
+#pragma unroll
+        for (int h = 8; h > 0; h >>= 1)
+#pragma unroll
+          for (int r = 0; r < h; ++r) vals[r] = cadd(vals[r], vals[r + h]);
+        wc = vals[0];
+      }
+      // ---- rank-1 update of the remaining panel columns
+      const double2 ctau = cconj(tau);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c > jj) {
+          const double2 wcc = c2(__shfl_sync(0xffffffffu, wc.x, c), __shfl_sync(0xffffffffu, wc.y, c));
+          const double2 f = cmul(ctau, wcc);
+#pragma unroll
+          for (int t = 0; t < ROWS; ++t) {
+            const int i = rb + t * 32 + lane;
+            if (apply && i >= col && i < re) {
+              const double2 vv = (i == col) ? c2(1.0, 0.0) : x[t][jj];
+              x[t][c] = csub(x[t][c], cmul(vv, f));
+            }
+          }
+        }
+      }
+    }
+  }
+
+  // ---- write the panel back and the explicit V
+#pragma unroll
+  for (int t = 0; t < ROWS; ++t) {
+    const int i = rb + t * 32 + lane;
+    if (i < re) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < jb) {
+          const int col = j0 + c;
+          a[(long)i * lda + col] = x[t][c];
+          V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x[t][c];
+        }
+      }
+    }
+  }
+  // ---- partial Gram G[p][c] = v_p^H v_c (p < c) over own rows
+#pragma unroll
+  for (int c = 1; c < NB; ++c) {
+    if (c < jb) {
+      double2 g[NB];
+#pragma unroll
+      for (int p = 0; p < NB; ++p) g[p] = c2(0.0, 0.0);
+#pragma unroll
+      for (int t = 0; t < ROWS; ++t) {
+        const int i = rb + t * 32 + lane;
+        if (i >= j0 + c && i < re) {
+          const double2 vc = (i == j0 + c) ? c2(1.0, 0.0) : x[t][c];
+#pragma unroll
+          for (int p = 0; p < NB; ++p) {
+            if (p < c) {
+              const double2 vp = (i == j0 + p) ? c2(1.0, 0.0) : x[t][p];
+              g[p] = cfma(cconj(vp), vc, g[p]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int p = 0; p < NB; ++p) {
+        if (p < c) {
+          g[p].x = wsum(g[p].x);
+          g[p].y = wsum(g[p].y);
+          if (lane == 0) s_G[p][c] = g[p];
+        }
+      }
+    }
+  }
+  cluster.sync();
+  if (rank == 0) {
+    // lane p gathers column entries p of the summed Gram as they are needed
+    double2 T[NB];   // lane p holds row p of T
+#pragma unroll
+    for (int c = 0; c < NB; ++c) T[c] = c2(0.0, 0.0);
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      if (c < jb) {
+        double2 gpc = c2(0.0, 0.0);
+        if (lane < c) {
+          double2 vals[16];
+#pragma unroll
+          for (int r = 0; r < 16; ++r)
+            vals[r] = (r < cs) ? cluster.map_shared_rank(&s_G[0][0], r)[lane * NB + c] : c2(0.0, 0.0);
+#pragma unroll
+          for (int h = 8; h > 0; h >>= 1)
+#pragma unroll
+            for (int q = 0; q < h; ++q) vals[q] = cadd(vals[q], vals[q + h]);
+          gpc = vals[0];
+        }
+        // T[p][c] = -tau_c sum_{q=p}^{c-1} T[p][q] G[q][c]; G[q][c] lives in lane q
+        double2 acc = c2(0.0, 0.0);
+#pragma unroll
+        for (int q = 0; q < NB; ++q) {
+          if (q < c) {
+            const double2 gqc = c2(__shfl_sync(0xffffffffu, gpc.x, q), __shfl_sync(0xffffffffu, gpc.y, q));
+            if (lane <= q) acc = cfma(T[q], gqc, acc);
+          }
+        }
+        const double2 tc = taus_l[c];
+        if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc);
+        if (lane == c) T[c] = tc;
+      }
+    }
+    if (lane < NB)
+#pragma unroll
+      for (int c = 0; c < NB; ++c) Tout[lane * NB + c] = T[c];
+  }
+  cluster.sync();   // no CTA leaves while its shared memory may still be read
+}
+
+// Panel factorisation for GB300's FP64 budget: a cluster of CS CTAs of 4 warps
+// (one per SM sub-partition, each with its own FP64 pipe), one panel row per
+// thread in registers. Per column: norm and dot products are reduced inside each
+// warp by reduce-scatter (lane l ends up with the warp sum of one value), across
+// the 4 warps through shared memory and across the cluster through distributed
+// shared memory, with two cluster barriers. The reflector scalars are computed by
+// every warp from the gathered partials (no broadcast). The dot products of the
+// new reflector with the previous ones (for T) ride along in the same reduction.
+constexpr int QW = 4;   // warps per CTA
+
+// 16 complex values per lane -> lane l holds the warp sum of value qv(l)
+__device__ __forceinline__ double2 reduce_scatter16(double2 (&v)[NB], int lane) {
+#pragma unroll
+  for (int lvl = 0, half = 8, mask = 16; lvl < 4; ++lvl, half >>= 1, mask >>= 1) {
+    const bool up = (lane & mask) != 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      if (i < half) {
+        const double2 send = up ? v[i] : v[i + half];
+        const double2 keep = up ? v[i + half] : v[i];
+        const double2 got = c2(__shfl_xor_sync(0xffffffffu, send.x, mask),
+                               __shfl_xor_sync(0xffffffffu, send.y, mask));
+        v[i] = cadd(keep, got);
+      }
+    }
+  }
+  const double2 r = v[0];
+  return cadd(r, c2(__shfl_xor_sync(0xffffffffu, r.x, 1), __shfl_xor_sync(0xffffffffu, r.y, 1)));
+}
+
+// value index held by lane after reduce_scatter16
+__device__ __forceinline__ int rs_index(int lane) {
+  return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+}
+
+__global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict__ a, long lda, int m,
+                                                            int j0, int jb,
+                                                            double2* __restrict__ Tout,
+                                                            double2* __restrict__ V, long ldv) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int cs = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  __shared__ double s_wn[QW];             // per-warp norm partials
+  __shared__ double2 s_wv[QW][2 * NB];    // per-warp vector partials (w and g)
+  __shared__ double s_nrm;                // CTA partial norm (read remotely)
+  __shared__ double2 s_alpha;
+  __shared__ double2 s_vec[2 * NB];       // CTA partial vectors (read remotely)
+  __shared__ double2 s_G[NB][NB];         // summed Gram (rank 0)
+
+  const int mp = m - j0;
+  const int chunk = (mp + cs - 1) / cs;
+  const int rb = j0 + rank * chunk;
+  const int re = min(m, rb + chunk);
+  const int i = rb + tid;                 // this thread's row
+  const bool mine = i < re;
+
+  double2 x[NB];
+#pragma unroll
+  for (int c = 0; c < NB; ++c) x[c] = (mine && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
+  double2 taus_l[NB];
+  double2 Gcol[NB];   // rank 0: G[p][c] for this thread's p = tid, filled per column c
+
+#pragma unroll
+  for (int jj = 0; jj < NB; ++jj) {
+    if (jj < jb) {
+      const int col = j0 + jj;
+      const int owner = jj / chunk;
+      // ---- norm
+      double acc = (mine && i > col) ? fma(x[jj].x, x[jj].x, x[jj].y * x[jj].y) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) s_wn[warp] = acc;
+      if (i == col) s_alpha = x[jj];
+      __syncthreads();
+      if (tid == 0) s_nrm = (s_wn[0] + s_wn[1]) + (s_wn[2] + s_wn[3]);
+      cluster.sync();
+      double v = (lane < cs) ? *cluster.map_shared_rank(&s_nrm, lane) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      const double xn2 = v;
+      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
+      double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
+      double beta = 0.0;
+      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
+      if (apply) {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        const double ib = 1.0 / beta;
+        tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
+        scal = crecip(c2(alpha.x - beta, alpha.y));
+      }
+      taus_l[jj] = tau;
+      if (apply && mine && i > col) x[jj] = cmul(x[jj], scal);
+      if (apply && i == col) x[jj] = c2(beta, 0.0);
+      // ---- one reduction: w_c = v^H a_c (c > jj) and g_p = v_p^H v (p < jj)
+      const double2 vcur = (mine && i >= col) ? ((i == col) ? c2(1.0, 0.0) : x[jj]) : c2(0.0, 0.0);
+      double2 q[NB];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c > jj) q[c] = cmul(cconj(vcur), x[c]);
+        else if (c < jj) {
+          const double2 vp = (mine && i >= j0 + c) ? ((i == j0 + c) ? c2(1.0, 0.0) : x[c]) : c2(0.0, 0.0);
+          q[c] = cmul(cconj(vp), vcur);
+        } else q[c] = c2(0.0, 0.0);
+      }
+      const double2 ws = reduce_scatter16(q, lane);
+      const int qi = rs_index(lane);
+      if ((lane & 1) == 0) s_wv[warp][qi] = ws;
+      __syncthreads();
+      if (tid < NB)
+        s_vec[tid] = cadd(cadd(s_wv[0][tid], s_wv[1][tid]), cadd(s_wv[2][tid], s_wv[3][tid]));
+      cluster.sync();
+      // ---- gather: lane c (< NB) of every warp sums rank by rank (tree, same order everywhere)
+      double2 tot = c2(0.0, 0.0);
+      if (lane < NB) {
+        double2 vals[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r)
+          vals[r] = (r < cs) ? cluster.map_shared_rank(s_vec, r)[lane] : c2(0.0, 0.0);
+#pragma unroll
+        for (int h = 8; h > 0; h >>= 1)
+#pragma unroll
+          for (int r = 0; r < h; ++r) vals[r] = cadd(vals[r], vals[r + h]);
+        tot = vals[0];
+      }
+      // Gram column jj for T (only rank 0 needs it): thread p keeps G[p][jj]
+      {
+        const double2 gp = c2(__shfl_sync(0xffffffffu, tot.x, lane & 15),
+                              __shfl_sync(0xffffffffu, tot.y, lane & 15));
+        if (tid < jj) Gcol[jj] = gp;
+      }
+      // ---- rank-1 update of this thread's row
+      const double2 ctau = cconj(tau);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c > jj) {
+          const double2 wcc = c2(__shfl_sync(0xffffffffu, tot.x, c), __shfl_sync(0xffffffffu, tot.y, c));
+          if (apply && mine && i >= col) x[c] = csub(x[c], cmul(vcur, cmul(ctau, wcc)));
+        }
+      }
+    }
+  }
+
+  // ---- write the panel back and the explicit V
+  if (mine) {
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      if (c < jb) {
+        const int col = j0 + c;
+        a[(long)i * lda + col] = x[c];
+        V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x[c];
+      }
+    }
+  }
+  // ---- T (zlarft) on rank 0 from the Gram columns kept by threads p < NB
+  if (rank == 0) {
+    if (tid < NB) {
+#pragma unroll
+      for (int c = 0; c < NB; ++c) s_G[tid][c] = (tid < c && c < jb) ? Gcol[c] : c2(0.0, 0.0);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      double2 T[NB];   // lane p holds row p of T
+#pragma unroll
+      for (int c = 0; c < NB; ++c) T[c] = c2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < jb) {
+          double2 acc2 = c2(0.0, 0.0);
+#pragma unroll
+          for (int qq = 0; qq < NB; ++qq)
+            if (qq < c && lane <= qq) acc2 = cfma(T[qq], s_G[qq][c], acc2);
+          const double2 tc = taus_l[c];
+          if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc2);
+          if (lane == c) T[c] = tc;
+        }
+      }
+      if (lane < NB)
+#pragma unroll
+        for (int c = 0; c < NB; ++c) Tout[lane * NB + c] = T[c];
+    }
+  }
+  cluster.sync();   // no CTA leaves while its shared memory may still be read
+}
+
 // partial[rb][j][c] = sum_{rows r of tile rb} conj(V[r][v0 + j]) C[r][c0 + c]
 // lane layout: tr = lane & 7 (row phase), 4 columns per warp, 8 warps -> 32 columns.
+template <int RTT, int CTT>
 __global__ void __launch_bounds__(256) larfb_partial_kernel(const double2* __restrict__ C, long ldc,
                                                             const double2* __restrict__ V, long ldv,
                                                             int r0, int m, int c0, int nc, int v0,
                                                             int jb, double2* __restrict__ part) {
-  __shared__ double2 sv[RT][NB];
+  __shared__ double2 sv[RTT][NB];
   const int rb = blockIdx.y;
-  const int rbase = r0 + rb * RT;
-  for (int idx = threadIdx.x; idx < RT * NB; idx += blockDim.x) {
+  const int rbase = r0 + rb * RTT;
+  for (int idx = threadIdx.x; idx < RTT * NB; idx += blockDim.x) {
     const int rr = idx / NB, j = idx % NB;
     const int r = rbase + rr;
     sv[rr][j] = (r < m && j < jb) ? V[(long)r * ldv + v0 + j] : c2(0.0, 0.0);
   }
   __syncthreads();
+  constexpr int CPW = CTT / 8;             // columns per warp
+  constexpr int RPH = 32 / CPW;            // row phases per column
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int tr = lane & 7;
-  const int cc = wid * 4 + (lane >> 3);
-  const int c = c0 + blockIdx.x * CTL + cc;
+  const int tr = lane % RPH;
+  const int cc = wid * CPW + lane / RPH;
+  const int c = c0 + blockIdx.x * CTT + cc;
   double2 acc[NB];
 #pragma unroll
   for (int j = 0; j < NB; ++j) acc[j] = c2(0.0, 0.0);
   if (c < c0 + nc) {
-    for (int rr = tr; rr < RT; rr += 8) {
+    for (int rr = tr; rr < RTT; rr += RPH) {
       const int r = rbase + rr;
       if (r >= m) break;
       const double2 x = C[(long)r * ldc + c];
@@ -209,7 +815,7 @@ __global__ void __launch_bounds__(256) larfb_partial_kernel(const double2* __res
 #pragma unroll
   for (int j = 0; j < NB; ++j) {
 #pragma unroll
-    for (int o = 1; o < 8; o <<= 1) {
+    for (int o = 1; o < RPH; o <<= 1) {
       acc[j].x += __shfl_xor_sync(0xffffffffu, acc[j].x, o);
       acc[j].y += __shfl_xor_sync(0xffffffffu, acc[j].y, o);
     }
@@ -222,35 +828,36 @@ __global__ void __launch_bounds__(256) larfb_partial_kernel(const double2* __res
 }
 
 // W = sum_rb partial; W2 = op(T) W (op = T^H if conjT else T); C -= V W2 on this tile
+template <int RTT, int CTT>
 __global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__ C, long ldc,
                                                            const double2* __restrict__ V, long ldv,
                                                            int r0, int m, int c0, int nc, int v0,
                                                            int jb, const double2* __restrict__ part,
                                                            int nrb, const double2* __restrict__ T,
                                                            int conjT) {
-  __shared__ double2 sv[RT][NB];
-  __shared__ double2 sw[NB][CTL];
-  __shared__ double2 sw2[NB][CTL];
+  __shared__ double2 sv[RTT][NB];
+  __shared__ double2 sw[NB][CTT];
+  __shared__ double2 sw2[NB][CTT];
   __shared__ double2 sT[NB][NB];
   const int rb = blockIdx.y;
-  const int rbase = r0 + rb * RT;
-  for (int idx = threadIdx.x; idx < RT * NB; idx += blockDim.x) {
+  const int rbase = r0 + rb * RTT;
+  for (int idx = threadIdx.x; idx < RTT * NB; idx += blockDim.x) {
     const int rr = idx / NB, j = idx % NB;
     const int r = rbase + rr;
     sv[rr][j] = (r < m && j < jb) ? V[(long)r * ldv + v0 + j] : c2(0.0, 0.0);
   }
   if (threadIdx.x < NB * NB) sT[threadIdx.x / NB][threadIdx.x % NB] = T[threadIdx.x];
-  for (int idx = threadIdx.x; idx < NB * CTL; idx += blockDim.x) {
-    const int j = idx / CTL, cc = idx % CTL;
-    const int c = blockIdx.x * CTL + cc;
+  for (int idx = threadIdx.x; idx < NB * CTT; idx += blockDim.x) {
+    const int j = idx / CTT, cc = idx % CTT;
+    const int c = blockIdx.x * CTT + cc;
     double2 s = c2(0.0, 0.0);
     if (j < jb && c < nc)
       for (int b = 0; b < nrb; ++b) s = cadd(s, part[((long)b * NB + j) * nc + c]);
     sw[j][cc] = s;
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < NB * CTL; idx += blockDim.x) {
-    const int j = idx / CTL, cc = idx % CTL;
+  for (int idx = threadIdx.x; idx < NB * CTT; idx += blockDim.x) {
+    const int j = idx / CTT, cc = idx % CTT;
     double2 s = c2(0.0, 0.0);
     if (j < jb) {
       if (conjT) {
@@ -262,10 +869,10 @@ __global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__
     sw2[j][cc] = s;
   }
   __syncthreads();
-  const int tc = threadIdx.x & 31, tr = threadIdx.x >> 5;
-  const int c = c0 + blockIdx.x * CTL + tc;
+  const int tc = threadIdx.x % CTT, tr = threadIdx.x / CTT;
+  const int c = c0 + blockIdx.x * CTT + tc;
   if (c >= c0 + nc) return;
-  for (int rr = tr; rr < RT; rr += 8) {
+  for (int rr = tr; rr < RTT; rr += 256 / CTT) {
     const int r = rbase + rr;
     if (r >= m) break;
     double2 x = C[(long)r * ldc + c];
@@ -316,16 +923,74 @@ QrWs carve_qr(void* ws, int m, int n) {
   return w;
 }
 
-ptn_status larfb(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
-                 int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
-  const int nrb = (m - r0 + RT - 1) / RT;
-  dim3 grid((nc + CTL - 1) / CTL, nrb);
-  larfb_partial_kernel<<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part);
-  larfb_update_kernel<<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part, nrb, T,
-                                            conjT ? 1 : 0);
+template <int RTT, int CTT>
+ptn_status larfb_t(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
+                   int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
+  const int nrb = (m - r0 + RTT - 1) / RTT;
+  dim3 grid((nc + CTT - 1) / CTT, nrb);
+  larfb_partial_kernel<RTT, CTT><<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part);
+  larfb_update_kernel<RTT, CTT><<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part,
+                                                      nrb, T, conjT ? 1 : 0);
   PTN_LAUNCH_CHECK();
   note_launches(2);
   return PTN_OK;
+}
+
+// the tile shape is chosen per call so that shrinking trailing matrices still
+// launch enough CTAs to keep every SM's FP64 pipes busy
+ptn_status larfb(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
+                 int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
+  const long rows = m - r0;
+  const long want = 2L * num_sms();
+  auto ctas = [&](long rt, long ct) { return ((rows + rt - 1) / rt) * ((nc + ct - 1) / ct); };
+  if (ctas(64, 32) >= want) return larfb_t<64, 32>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+  if (ctas(32, 32) >= want) return larfb_t<32, 32>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+  if (ctas(32, 16) >= want) return larfb_t<32, 16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+  return larfb_t<16, 16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+}
+
+}  // namespace
+
+namespace {
+
+// Largest cluster the panel kernel can be launched with on this device (16, else 8,
+// else 1 = the single-CTA kernel); decided once.
+int panel_cluster_size() {
+  static int cs = 0;
+  if (cs != 0) return cs;
+  cs = 1;
+  if (cudaFuncSetAttribute(qr_panel_cluster_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                           1) != cudaSuccess)
+    cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel4_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess)
+    cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel_warp_kernel<1>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                           1) != cudaSuccess)
+    cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel_warp_kernel<2>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                           1) != cudaSuccess)
+    cudaGetLastError();
+  for (int c : {16, 8}) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(c);
+    cfg.blockDim = dim3(CPT);
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = c;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, qr_panel_cluster_kernel, &cfg) == cudaSuccess &&
+        nclusters > 0) {
+      cs = c;
+      break;
+    }
+    cudaGetLastError();
+  }
+  return cs;
 }
 
 }  // namespace
@@ -333,7 +998,7 @@ ptn_status larfb(double2* C, long ldc, const double2* V, long ldv, int r0, int m
 size_t qr_workspace_bytes(int m, int n) {
   const int k = std::min(m, n);
   const int np = (k + NB - 1) / NB;
-  const int nrb = (m + RT - 1) / RT;
+  const int nrb = (m + 15) / 16;   // smallest row tile of the block update
   return al((size_t)m * k * sizeof(double2)) + al((size_t)np * NB * NB * sizeof(double2)) +
          al((size_t)nrb * NB * std::max(n, k) * sizeof(double2));
 }
@@ -348,9 +1013,62 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
   // LAPACK flop count of zgeqrf + zungqr (4 real flops per complex op)
   const double fq = 8.0 * ((double)m * n * k - (double)(m + n) * k * k / 2.0 + (double)k * k * k / 3.0);
   const int prof = prof_begin(st, PROF_QR, 2.0 * fq, 16.0 * 3.0 * m * n);
+  const int cs = panel_cluster_size();
   for (int j0 = 0, p = 0; j0 < k; j0 += NB, ++p) {
     const int jb = std::min(NB, k - j0);
-    qr_panel_kernel<<<1, PT, 0, st>>>(a, lda, m, j0, jb, w.T + (long)p * NB * NB, w.V, k);
+    const int chunk = cs > 1 ? (m - j0 + cs - 1) / cs : m - j0;
+    if (cs > 1 && chunk <= QW * 32) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(QW * 32);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel4_kernel, a, lda, m, j0, jb,
+                                      w.T + (long)p * NB * NB, w.V, (long)k));
+    } else if (cs > 1 && chunk <= 64) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(32);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      if (chunk <= 32)
+        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_warp_kernel<1>, a, lda, m, j0, jb,
+                                        w.T + (long)p * NB * NB, w.V, (long)k));
+      else
+        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_warp_kernel<2>, a, lda, m, j0, jb,
+                                        w.T + (long)p * NB * NB, w.V, (long)k));
+    } else if (cs > 1) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(cs);
+      cfg.blockDim = dim3(CPT);
+      cfg.dynamicSmemBytes = 0;
+      cfg.stream = st;
+      cudaLaunchAttribute attr[1];
+      attr[0].id = cudaLaunchAttributeClusterDimension;
+      attr[0].val.clusterDim.x = cs;
+      attr[0].val.clusterDim.y = 1;
+      attr[0].val.clusterDim.z = 1;
+      cfg.attrs = attr;
+      cfg.numAttrs = 1;
+      PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_cluster_kernel, a, lda, m, j0, jb,
+                                      w.T + (long)p * NB * NB, w.V, (long)k));
+    } else {
+      qr_panel_kernel<<<1, PT, 0, st>>>(a, lda, m, j0, jb, w.T + (long)p * NB * NB, w.V, k);
+    }
     PTN_LAUNCH_CHECK();
     note_launches(1);
     const int nc = n - j0 - jb;
