@@ -9,7 +9,13 @@ resident in HBM when the timed region starts; the whole state (site tensors,
 environments, Krylov basis: several GB) is far larger than the 129 MB L2, so no
 explicit L2 flush is needed between steps.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form mixed|fp64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form learned|mixed|fp64]
+
+Forms: "fp64" = complex128 everywhere, fixed Lanczos depth (the reference's
+method); "mixed" = split-BF16 tensor-core contractions (exact fixed-point digits,
+FP32 accumulation, FP64 recombination) with FP64 Krylov / QR, fixed depth;
+"learned" (default) = "mixed" plus the learned Lanczos depth (trained MLP,
+residual-guarded early exit, falling back to the full depth).
   python bench.py --impl reference ...   # the reference CPU algorithm (NumPy oracle
                                          # port) on this host's cores, same metric
 
@@ -40,8 +46,9 @@ def parse():
     p.add_argument("--steps", type=int, default=None)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    p.add_argument("--form", default=os.environ.get("PTN_BENCH_FORM", "mixed"),
-                   choices=["mixed", "fp64"])
+    p.add_argument("--form", default=os.environ.get("PTN_BENCH_FORM", "learned"),
+                   choices=["learned", "mixed", "fp64"])
+    p.add_argument("--depth-tol", type=float, default=1e-10)
     p.add_argument("--L", type=int, default=64)
     p.add_argument("--D", type=int, default=512)
     p.add_argument("--m", type=int, default=10)
@@ -54,7 +61,7 @@ def parse():
     p.add_argument("--graph", action="store_true")
     a = p.parse_args()
     if a.steps is None:
-        a.steps = 5 if a.form == "mixed" else 1
+        a.steps = 1 if a.form == "fp64" else 5
     assert a.warmup >= 3, "at least 3 warm-up steps"
     return a
 
@@ -233,7 +240,13 @@ def our_arm(a):
     qb0 = [q.copy() for q in psi.qbonds]
     site_updates = 2 * a.L - 1
 
-    run = ptg.TDVPRun(h, psi, numiter_lanczos=a.m, precision=a.form, graph=a.graph)
+    prec = "fp64" if a.form == "fp64" else "mixed"
+    depth_model = None
+    if a.form == "learned":
+        from pytenet_gb300.learned import DepthModel
+        depth_model = DepthModel.load()
+    run = ptg.TDVPRun(h, psi, numiter_lanczos=a.m, precision=prec, graph=a.graph,
+                      depth_model=depth_model, depth_tol=a.depth_tol)
     dt = 0.05j
     for _ in range(a.warmup):
         run.step(dt)
@@ -243,7 +256,8 @@ def our_arm(a):
     clocks = ClockSampler(local)
     clocks.start()
     launches0 = L.ptn_launch_count()
-    dominant = 1 if a.form == "mixed" else 0
+    dominant = 0 if a.form == "fp64" else 1
+    ks0 = run.chain.krylov_state()
     L.ptn_prof_start((1 << dominant) | (1 << 3))
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -257,6 +271,12 @@ def our_arm(a):
         dist.barrier()
     L.ptn_prof_stop()
     launches = L.ptn_launch_count() - launches0
+    ks1 = run.chain.krylov_state()
+    nlocal = a.steps * (2 * a.L - 1 + 2 * (a.L - 1))
+    krylov = {"local_steps": nlocal, "lanczos_iterations": ks1.iters_total - ks0.iters_total,
+              "mean_depth": (ks1.iters_total - ks0.iters_total) / nlocal,
+              "early_exits": ks1.early_exits - ks0.early_exits, "full_depth": a.m,
+              "depth_tol": a.depth_tol if a.form == "learned" else None}
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     t = torch.tensor([ms], dtype=torch.float64, device="cuda")
@@ -301,8 +321,8 @@ def our_arm(a):
 
     # ---- accuracy of the mixed form vs the FP64 form (same initial state)
     accuracy = None
-    if a.form == "mixed" and not a.no_accuracy and rank == 0:
-        accuracy = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0)
+    if a.form != "fp64" and not a.no_accuracy and rank == 0:
+        accuracy = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model)
 
     # ---- e2e through the public API with host buffers
     e2e = None
@@ -314,7 +334,8 @@ def our_arm(a):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
         for _ in range(a.e2e_steps):
-            ptg.tdvp_singlesite(h, psi_e, dt, 1, numiter_lanczos=a.m, precision=a.form)
+            ptg.tdvp_singlesite(h, psi_e, dt, 1, numiter_lanczos=a.m, precision=prec,
+                                depth_model=depth_model, depth_tol=a.depth_tol)
         torch.cuda.synchronize()
         et = time.perf_counter() - t0
         e2e = {"value": world * site_updates * a.e2e_steps / et, "unit": "site-updates/s",
@@ -341,23 +362,26 @@ def our_arm(a):
                           "numiter_lanczos": a.m, "delta": delta, "graph": a.graph,
                           "parallelism": f"replicas x{world}",
                           "l2": "inputs larger than L2 (state of several GB per replica)"},
-               "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
+               "krylov": krylov, "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
                "cpu_baseline": cpu, "accuracy_vs_fp64": accuracy}
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
 
 
-def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0):
-    """Energy error, infidelity and norm drift of the mixed form against the FP64
-    form after `--acc-steps` steps from the same initial state."""
+def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
+    """Energy error, infidelity and norm drift of the benchmarked form (mixed, with
+    the learned depth when given) against the plain FP64 fixed-depth form after
+    `--acc-steps` steps from the same initial state."""
     from pytenet_gb300.chain_ops import mpo_average, mps_vdot
     out = {}
     runs = {}
     for form in ("mixed", "fp64"):
         p = ptg.MPS(h.qsite, qb0, fill="postpone")
         p.a = [x.copy() for x in psi_host0]
-        r = ptg.TDVPRun(h, p, numiter_lanczos=a.m, precision=form)
+        r = ptg.TDVPRun(h, p, numiter_lanczos=a.m, precision=form,
+                        depth_model=depth_model if form == "mixed" else None,
+                        depth_tol=a.depth_tol)
         for _ in range(a.acc_steps):
             r.step(0.05j)
         r.download()
@@ -366,7 +390,7 @@ def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0):
     e_m, e_f = mpo_average(pm, h).real, mpo_average(pf, h).real
     ov = mps_vdot(pf, pm)
     nm2, nf2 = mps_vdot(pm, pm).real, mps_vdot(pf, pf).real
-    out = {"steps": a.acc_steps, "energy_fp64": e_f, "energy_mixed": e_m,
+    out = {"steps": a.acc_steps, "against": "fp64, fixed depth", "energy_fp64": e_f, "energy_mixed": e_m,
            "energy_rel_err": abs(e_m - e_f) / max(abs(e_f), 1e-300),
            "infidelity": 1.0 - abs(ov) ** 2 / (nm2 * nf2),
            "norm_drift": abs(np.sqrt(nm2) - np.sqrt(nf2))}

@@ -177,10 +177,47 @@ class DeviceMPS:
         raise ValueError(f'`mode` = {mode} invalid; must be "left" or "right".')
 
 
+class DepthState:
+    """Device buffers of the learned Lanczos depth: per-(site, kind) history of
+    the previous alpha / beta, the MLP parameters (or None: fixed depth), and an
+    optional training-record log."""
+
+    def __init__(self, nsites, params=None, tol=1e-10, log_capacity=0):
+        self.history = torch.zeros((2 * nsites, 8), dtype=torch.float32, device=device())
+        self.params = params
+        self.tol = float(tol)
+        self.log = None
+        self.log_count = None
+        self.log_capacity = int(log_capacity)
+        if log_capacity > 0:
+            self.log = torch.zeros((log_capacity, _lib.DEPTH_RECORD), dtype=torch.float64,
+                                   device=device())
+            self.log_count = torch.zeros(1, dtype=torch.int32, device=device())
+        self.nsites = nsites
+
+    def ctx(self, site, kind):
+        c = _lib.DepthCtx()
+        c.params = ptr(self.params) if self.params is not None else None
+        c.history = ptr(self.history)
+        c.slot = 2 * site + kind
+        c.site = site
+        c.nsites = self.nsites
+        c.kind = kind
+        c.tol = self.tol
+        c.log = ptr(self.log) if self.log is not None else None
+        c.log_count = ptr(self.log_count) if self.log_count is not None else None
+        c.log_capacity = self.log_capacity
+        return c
+
+    def records(self):
+        n = min(int(self.log_count.item()), self.log_capacity)
+        return self.log[:n]
+
+
 class Chain(DeviceMPS):
     """Device state of one TDVP / DMRG run: MPS, MPO, environments, Krylov buffers."""
 
-    def __init__(self, op, psi, numiter, precision="fp64"):
+    def __init__(self, op, psi, numiter, precision="fp64", depth=None):
         assert len(op.a) == len(psi.a)
         super().__init__(psi)
         self.prec = prec_code(precision)
@@ -212,6 +249,7 @@ class Chain(DeviceMPS):
                        L.ptn_bond_step_workspace_bytes(Dl, Dl, cl, self.prec))
         self.cws_bytes = need
         self.cws.get(need)
+        self.depth = depth
 
     # ---------------------------------------------------------------- envs
     def lview(self, i):
@@ -271,16 +309,28 @@ class Chain(DeviceMPS):
         cl, cr = self.chi[i], self.chi[i + 1]
         z = -complex(dt)
         ws = self.cws.get(self.cws_bytes)
+        if self.depth is not None:
+            ctx = self.depth.ctx(i, 0)
+            call(L.ptn_expm_site_ex, ptr(self.buf[i]), ptr(self.w[i]), ptr(self.lenv[i]),
+                 ptr(self.renv[i]), Dl, d, Dr, cl, cr, z.real, z.imag, self.numiter, self.prec,
+                 _lib.C.byref(ctx), ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
+            return
         call(L.ptn_expm_site, ptr(self.buf[i]), ptr(self.w[i]), ptr(self.lenv[i]),
              ptr(self.renv[i]), Dl, d, Dr, cl, cr, z.real, z.imag, self.numiter, self.prec,
              ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
 
-    def bond_expm(self, c, l, r, chi, dt):
+    def bond_expm(self, c, l, r, chi, dt, site=0):
         """c = expm(-dt H_bond) c (_local_bond_step, tdvp.py:232-238)."""
         L, st = lib(), stream_ptr()
         Dl, Dr = c.shape
         z = -complex(dt)
         ws = self.cws.get(self.cws_bytes)
+        if self.depth is not None:
+            ctx = self.depth.ctx(site, 1)
+            call(L.ptn_expm_bond_ex, ptr(c), ptr(l), ptr(r), Dl, Dr, chi, z.real, z.imag,
+                 self.numiter, self.prec, _lib.C.byref(ctx), ptr(self.V), ptr(self.state),
+                 ptr(ws), self.cws_bytes, st)
+            return
         call(L.ptn_expm_bond, ptr(c), ptr(l), ptr(r), Dl, Dr, chi, z.real, z.imag, self.numiter,
              self.prec, ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
 
@@ -302,13 +352,13 @@ class Chain(DeviceMPS):
             self.site_expm(i, 0.5 * dt)
             c = self.qr_left(i)
             self.env_left(i)
-            self.bond_expm(c, self.lenv[i + 1], self.renv[i], self.chi[i + 1], -0.5 * dt)
+            self.bond_expm(c, self.lenv[i + 1], self.renv[i], self.chi[i + 1], -0.5 * dt, site=i)
             self.absorb_left(c, i + 1)
         self.site_expm(n - 1, dt)
         for i in reversed(range(1, n)):
             c = self.qr_right(i)
             self.env_right(i)
-            self.bond_expm(c, self.lenv[i], self.renv[i - 1], self.chi[i], -0.5 * dt)
+            self.bond_expm(c, self.lenv[i], self.renv[i - 1], self.chi[i], -0.5 * dt, site=i - 1)
             self.absorb_right(c, i - 1)
             self.site_expm(i - 1, 0.5 * dt)
 
@@ -333,9 +383,12 @@ class Chain(DeviceMPS):
         off = getattr(_lib.KrylovState, name).offset
         return self.state[off:off + 8].view(torch.float64)
 
+    def krylov_state(self):
+        raw = bytes(self.state[: _lib.C.sizeof(_lib.KrylovState)].cpu().numpy())
+        return _lib.KrylovState.from_buffer_copy(raw)
+
     def breakdowns(self):
-        s = _lib.KrylovState.from_buffer_copy(bytes(self.state[: _lib.C.sizeof(_lib.KrylovState)].cpu().numpy()))
-        return s.breakdowns
+        return self.krylov_state().breakdowns
 
 
 def warn_breakdowns(chain):

@@ -14,16 +14,25 @@ class TDVPRun:
     """Device-resident TDVP run: upload once, step many times, download when
     asked. `tdvp_singlesite` is this class driven for `numsteps` steps.
 
-    precision: "fp64" (plain complex128) or "mixed" (split-BF16 contractions on
-    the tensor cores, FP64 Krylov / QR / environments).
+    precision: "fp64" (plain complex128) or "mixed" (fixed-point BF16 digit
+    contractions on the tensor cores, FP64 Krylov / QR).
+    depth_model: a trained learned.DepthModel; numiter_lanczos is then the full
+    depth the run falls back to whenever the residual estimate at the predicted
+    depth exceeds depth_tol.
     graph: capture one time step in a CUDA graph after the first step and
     replay it (all buffers are preallocated and no step synchronises)."""
 
-    def __init__(self, hamiltonian, psi, numiter_lanczos=25, precision="fp64", graph=False):
+    def __init__(self, hamiltonian, psi, numiter_lanczos=25, precision="fp64", graph=False,
+                 depth_model=None, depth_tol=1e-10, record_capacity=0):
         nsites = len(hamiltonian.a)
         assert nsites == len(psi.a)
         self.psi = psi
-        self.chain = Chain(hamiltonian, psi, numiter_lanczos, precision)
+        depth = None
+        if depth_model is not None or record_capacity > 0:
+            from .engine import DepthState
+            params = depth_model.params if depth_model is not None else None
+            depth = DepthState(nsites, params, depth_tol, record_capacity)
+        self.chain = Chain(hamiltonian, psi, numiter_lanczos, precision, depth=depth)
         # right-normalise, build the environments (pytenet/tdvp.py:51-63)
         self.nrm = self.chain.orthonormalize("right").clone()
         self.chain.init_envs()
@@ -72,11 +81,11 @@ class TDVPRun:
 
 
 def tdvp_singlesite(hamiltonian, psi, dt, numsteps, numiter_lanczos=25, precision="fp64",
-                    graph=False):
+                    graph=False, depth_model=None, depth_tol=1e-10):
     """Symmetric single-site TDVP; `psi` is overwritten in place with the evolved
     state and the norm of the initial `psi` is returned (pytenet/tdvp.py:26-118).
     All numerics run on the GPU."""
-    run = TDVPRun(hamiltonian, psi, numiter_lanczos, precision, graph)
+    run = TDVPRun(hamiltonian, psi, numiter_lanczos, precision, graph, depth_model, depth_tol)
     done = 0
     while done < numsteps:
         before = run.steps_done

@@ -147,3 +147,19 @@ def test_dmrg_singlesite():
     v = orc.mps_to_vector(psi)
     # eigenvector up to a global phase
     assert abs(abs(np.vdot(v, g["v1"])) - 1) < 1e-10
+
+
+def test_mlp_oracle_gradient_by_finite_differences():
+    """Pin the NumPy MLP checker itself: analytic gradient vs central differences."""
+    from oracle import mlp_oracle
+    rng = np.random.default_rng(0)
+    p = rng.normal(0, 0.3, 5057)
+    X = rng.normal(size=(7, 12))
+    T = rng.uniform(size=7)
+    g, loss = mlp_oracle.mlp_grad(p, X, T)
+    for idx in [0, 5, 770, 900, 4900, 4950, 5000, 5056]:
+        e = np.zeros_like(p)
+        e[idx] = 1e-6
+        fd = (np.mean((mlp_oracle.mlp_forward(p + e, X) - T) ** 2) -
+              np.mean((mlp_oracle.mlp_forward(p - e, X) - T) ** 2)) / 2e-6
+        assert abs(fd - g[idx]) < 1e-6 * max(1.0, abs(g[idx]))
