@@ -38,6 +38,7 @@ struct KState {
   double part_a[RED_MAX];
   double part_b[RED_MAX];
   int nblocks;                  // CTAs used by the vector passes of this run
+  int coef_ready;               // an accepted learned depth already stored coef[]
 };
 
 __device__ __forceinline__ double reduce_partials(const double* part, int nb, double* sh) {
@@ -89,6 +90,7 @@ __global__ void __launch_bounds__(VT) k_start_finish(KState* st, const double2* 
       st->s.eval0 = 0.0;
       st->s.resid = 0.0;
       st->s.m_target = 0;
+      st->coef_ready = 0;
       st->nblocks = nb;
     }
   }
@@ -229,12 +231,119 @@ __device__ void tridiag_ql(double* d, double* e, int n, double* z) {
   }
 }
 
+// c = nrm exp(dt T) e_1 for the m x m symmetric tridiagonal T (diagonal alpha,
+// off-diagonal beta[0..m-2]), by one warp: lane l holds entries l and l + 32.
+// Scaling and Taylor on the vector: with h = dt / 2^s and |h| |T|_1 <= 1/2, each of
+// the 2^s factors exp(h T) is summed to degree 16 (remainder below 2e-20 of the
+// vector). exp(dt T) e_1 is the same vector U exp(dt Lambda) U^T e_1 that
+// expm_krylov forms from eigh (pytenet/krylov.py:133-136); here it costs a chain of
+// tridiagonal products instead of the serial FP64 sqrt / division chain of a QL
+// eigensolver. Writes out[0..m-1] when out != null; returns c_{m-1} to all lanes.
+// Beyond |dt| |T|_1 > 2^(EXPM_MAX_SCALE - 1) it does nothing and returns ok = false
+// (the caller then takes the eigen-decomposition route or the full depth).
+constexpr int EXPM_MAX_SCALE = 12;
+__device__ double2 expm_e1_warp(const double* alpha, const double* beta, int m, double nrm,
+                                double dt_re, double dt_im, ptn_c128* out, bool& ok) {
+  const int lane = threadIdx.x & 31;
+  double a[2], bl[2], br[2];   // diagonal, left and right off-diagonal of my rows
+  double tn = 0.0;
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int k = lane + 32 * q;
+    a[q] = (k < m) ? alpha[k] : 0.0;
+    bl[q] = (k < m && k > 0) ? beta[k - 1] : 0.0;
+    br[q] = (k < m - 1) ? beta[k] : 0.0;
+    tn = fmax(tn, fabs(a[q]) + fabs(bl[q]) + fabs(br[q]));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) tn = fmax(tn, __shfl_xor_sync(0xffffffffu, tn, o));
+  const double dta = sqrt(dt_re * dt_re + dt_im * dt_im);
+  int sc = 0;
+  double nt = dta * tn;
+  while (nt > 0.5 && sc <= EXPM_MAX_SCALE) {
+    nt *= 0.5;
+    ++sc;
+  }
+  ok = (sc <= EXPM_MAX_SCALE) && (nt == nt);
+  if (!ok) return make_double2(0.0, 0.0);
+  const double hs = ldexp(1.0, -sc);
+  const double hr = dt_re * hs, hi = dt_im * hs;
+  // v = e_1
+  double vr[2] = {lane == 0 ? 1.0 : 0.0, 0.0}, vi[2] = {0.0, 0.0};
+  const long reps = 1L << sc;
+  for (long rep = 0; rep < reps; ++rep) {
+    double yr[2] = {vr[0], vr[1]}, yi[2] = {vi[0], vi[1]};
+    double tr[2] = {vr[0], vr[1]}, ti[2] = {vi[0], vi[1]};
+    for (int k = 1; k <= 16; ++k) {
+      // neighbours: entry k-1 and k+1 of both halves
+      double pr[2], pi[2], nr[2], ni[2];
+      const double up_r0 = __shfl_up_sync(0xffffffffu, tr[0], 1), up_i0 = __shfl_up_sync(0xffffffffu, ti[0], 1);
+      const double up_r1 = __shfl_up_sync(0xffffffffu, tr[1], 1), up_i1 = __shfl_up_sync(0xffffffffu, ti[1], 1);
+      const double dn_r0 = __shfl_down_sync(0xffffffffu, tr[0], 1), dn_i0 = __shfl_down_sync(0xffffffffu, ti[0], 1);
+      const double dn_r1 = __shfl_down_sync(0xffffffffu, tr[1], 1), dn_i1 = __shfl_down_sync(0xffffffffu, ti[1], 1);
+      const double w31_r0 = __shfl_sync(0xffffffffu, tr[0], 31), w31_i0 = __shfl_sync(0xffffffffu, ti[0], 31);
+      const double w0_r1 = __shfl_sync(0xffffffffu, tr[1], 0), w0_i1 = __shfl_sync(0xffffffffu, ti[1], 0);
+      pr[0] = lane > 0 ? up_r0 : 0.0;
+      pi[0] = lane > 0 ? up_i0 : 0.0;
+      pr[1] = lane > 0 ? up_r1 : w31_r0;
+      pi[1] = lane > 0 ? up_i1 : w31_i0;
+      nr[0] = lane < 31 ? dn_r0 : w0_r1;
+      ni[0] = lane < 31 ? dn_i0 : w0_i1;
+      nr[1] = lane < 31 ? dn_r1 : 0.0;
+      ni[1] = lane < 31 ? dn_i1 : 0.0;
+      const double inv = 1.0 / (double)k;
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        // u = T t (real T), then t <- (h / k) u
+        const double ur = fma(bl[q], pr[q], fma(a[q], tr[q], br[q] * nr[q]));
+        const double ui = fma(bl[q], pi[q], fma(a[q], ti[q], br[q] * ni[q]));
+        const double cr = hr * inv, ci = hi * inv;
+        tr[q] = fma(cr, ur, -ci * ui);
+        ti[q] = fma(cr, ui, ci * ur);
+        yr[q] += tr[q];
+        yi[q] += ti[q];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      const int kk = lane + 32 * q;
+      vr[q] = (kk < m) ? yr[q] : 0.0;
+      vi[q] = (kk < m) ? yi[q] : 0.0;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 2; ++q) {
+    const int k = lane + 32 * q;
+    if (out != nullptr && k < m) {
+      out[k].re = nrm * vr[q];
+      out[k].im = nrm * vi[q];
+    }
+  }
+  const int ql = (m - 1) >> 5, ll = (m - 1) & 31;
+  const double lr = __shfl_sync(0xffffffffu, ql ? vr[1] : vr[0], ll);
+  const double li = __shfl_sync(0xffffffffu, ql ? vi[1] : vi[0], ll);
+  return make_double2(nrm * lr, nrm * li);
+}
+
 // mode 0: expm coefficients c = nrm U exp(dt Lambda) U^T e_1;
 // mode 1: lowest Ritz vector coefficients c = U[:, argmin], eval0 = min eigenvalue.
 __global__ void k_tridiag(KState* st, double dt_re, double dt_im, int mode) {
   const int lane = threadIdx.x;  // one warp
   if (st->s.status != PTN_OK) return;
   const int m = st->s.m_used;
+  bool ok = true;
+  if (mode == 0 && !st->coef_ready)
+    expm_e1_warp(st->s.alpha, st->s.beta, m, st->s.nrm, dt_re, dt_im, st->s.coef, ok);
+  if (mode == 0 && ok) {
+    __syncwarp();
+    if (lane == 0) {
+      const ptn_c128 cl = st->s.coef[m - 1];
+      // an accepted learned depth already stored its relative estimate
+      if (!st->coef_ready) st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im);
+      st->s.iters_total += m;
+    }
+    return;
+  }
   double d[PTN_KRYLOV_MAXITER], e[PTN_KRYLOV_MAXITER], z[PTN_KRYLOV_MAXITER];
   for (int i = 0; i < m; ++i) {
     d[i] = st->s.alpha[i];
@@ -289,32 +398,12 @@ __global__ void k_tridiag(KState* st, double dt_re, double dt_im, int mode) {
 // ------------------------------------------------------------------ learned depth
 typedef ptn_depth_ctx DepthArgs;
 
-// c_{m-1} of nrm * U exp(dt Lambda) U^T e_1 for the leading m x m block (all lanes
-// get the value); alpha / beta from the given arrays
+// c_{m-1} of nrm exp(dt T_m) e_1 for the leading m x m block (all lanes get it)
 __device__ double2 last_coef(const double* alpha, const double* beta, int m, double nrm,
                              double dt_re, double dt_im) {
-  const int lane = threadIdx.x & 31;
-  double d[PTN_KRYLOV_MAXITER], e[PTN_KRYLOV_MAXITER], z[PTN_KRYLOV_MAXITER];
-  for (int i = 0; i < m; ++i) {
-    d[i] = alpha[i];
-    e[i] = (i < m - 1) ? beta[i] : 0.0;
-  }
-  // lane 0 carries row 0 of U, lane 1 row m-1 (m >= 2), others idle copies
-  const int row = (lane == 1) ? m - 1 : 0;
-  for (int i = 0; i < m; ++i) z[i] = (i == row) ? 1.0 : 0.0;
-  tridiag_ql(d, e, m, z);
-  double cr = 0.0, ci = 0.0;
-  for (int j = 0; j < m; ++j) {
-    const double u0 = __shfl_sync(0xffffffffu, z[j], 0);
-    const double ul = __shfl_sync(0xffffffffu, z[j], 1);
-    const double a = exp(dt_re * d[j]);
-    double sn, cs;
-    sincos(dt_im * d[j], &sn, &cs);
-    const double f = nrm * u0 * ul * a;
-    cr = fma(f, cs, cr);
-    ci = fma(f, sn, ci);
-  }
-  return make_double2(cr, ci);
+  bool ok;
+  const double2 c = expm_e1_warp(alpha, beta, m, nrm, dt_re, dt_im, nullptr, ok);
+  return ok ? c : make_double2(HUGE_VAL, 0.0);   // no estimate: never accepted
 }
 
 // after iteration 0: features of this local step, and the predicted depth
@@ -352,14 +441,19 @@ __global__ void k_depth_check(KState* st, int j, double dt_re, double dt_im, dou
   if (st->s.stopped || st->s.m_target != j + 1) return;
   const int m = j + 1;
   const double nrm = st->s.nrm;
-  const double2 c = last_coef(st->s.alpha, st->s.beta, m, nrm, dt_re, dt_im);
-  const double est = st->s.beta[j] * sqrt(c.x * c.x + c.y * c.y) / nrm;
+  // coefficients of the truncated run straight into coef[]: used as they are if
+  // the depth is accepted, overwritten by the full-depth run otherwise
+  bool ok;
+  const double2 c = expm_e1_warp(st->s.alpha, st->s.beta, m, nrm, dt_re, dt_im, st->s.coef, ok);
+  const double est = ok ? st->s.beta[j] * sqrt(c.x * c.x + c.y * c.y) / nrm : HUGE_VAL;
+  __syncwarp();
   if (threadIdx.x == 0) {
     if (est <= tol) {
       st->s.m_used = m;
       st->s.stopped = 1;
       st->s.early_exits += 1;
       st->s.resid = est;
+      st->coef_ready = 1;
     } else {
       st->s.m_target = 0;   // fall back to the full depth
     }

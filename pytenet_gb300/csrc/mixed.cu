@@ -63,6 +63,10 @@ __device__ __forceinline__ void load_tile(double2 (*tile)[33], const double2* __
   }
 }
 
+__device__ __forceinline__ int biased_exp(double x) {
+  return (int)((__double_as_longlong(x) >> 52) & 0x7FF);
+}
+
 __global__ void rowexp_kernel(const double2* __restrict__ src, long sr, long sk, int R, int K,
                               int* __restrict__ e, const int* skip) {
   if (skip != nullptr && *skip != 0) return;
@@ -72,25 +76,41 @@ __global__ void rowexp_kernel(const double2* __restrict__ src, long sr, long sk,
   __syncthreads();
   for (int rr = threadIdx.y; rr < 32; rr += 8) {
     const double2 v = tile[rr][threadIdx.x];
-    double m = fmax(fabs(v.x), fabs(v.y));
+    // biased exponent fields (integer work only; zero and subnormal entries give 0)
+    int m = max(biased_exp(v.x), biased_exp(v.y));
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if (threadIdx.x == 0 && r0 + rr < R && m > 0.0) {
-      int ex;
-      frexp(m, &ex);   // m = f 2^ex with f in [0.5, 1): every |entry| < 2^ex
-      atomicMax(&e[r0 + rr], ex);
+    for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (threadIdx.x == 0 && r0 + rr < R && m > 0) {
+      // a normal |x| with biased exponent E lies in [2^(E-1023), 2^(E-1022)): every
+      // entry of the row is below 2^ex (frexp's exponent of the largest one)
+      atomicMax(&e[r0 + rr], m - 1022);
     }
   }
 }
 
-__device__ __forceinline__ void digits4(double x, double scale, bf16 (&d)[NDIGIT]) {
-  double t = x * scale;   // exact: power of two
-#pragma unroll
-  for (int i = 0; i < NDIGIT; ++i) {
-    const double q = rint(t);
-    d[i] = __double2bfloat16(q);   // |q| <= 128: exact in BF16
-    t = (t - q) * 256.0;           // exact
+// Balanced base-256 digits of x 2^(7 - ex) (|x| < 2^ex): the fixed-point integer
+// T = round(x 2^(31 - ex)) (|T| <= 2^31) is cut into T = d0 2^24 + d1 2^16 + d2 2^8 + d3
+// with d1..d3 in [-128, 127] and |d0| <= 128, each exact in BF16. Integer
+// arithmetic on the IEEE fields only: the CUDA-core FP64 rate of this part is low.
+// Zero and subnormal entries (below 2^-1022) give zero digits.
+__device__ __forceinline__ void digits4(double x, int ex, bf16 (&d)[NDIGIT]) {
+  const long long b = __double_as_longlong(x);
+  const int E = (int)((b >> 52) & 0x7FF);
+  long long T = 0;
+  if (E != 0) {
+    const long long mant = (b & ((1LL << 52) - 1)) | (1LL << 52);
+    // x = mant 2^(E - 1075): T = round(mant 2^(E - 1075 + 31 - ex)), shift always right
+    const int rs = 1075 - 31 + ex - E;
+    if (rs < 63) T = (rs <= 0) ? (mant << (-rs)) : ((mant + (1LL << (rs - 1))) >> rs);
+    if (b < 0) T = -T;
   }
+#pragma unroll
+  for (int i = NDIGIT - 1; i > 0; --i) {
+    const int di = (int)((T + 128) & 255) - 128;
+    d[i] = __int2bfloat16_rn(di);
+    T = (T - di) >> 8;   // exact
+  }
+  d[0] = __int2bfloat16_rn((int)T);
 }
 
 __global__ void digits_kernel(const double2* __restrict__ src, long sr, long sk, int R, int K,
@@ -110,9 +130,8 @@ __global__ void digits_kernel(const double2* __restrict__ src, long sr, long sk,
     const double2 z = tile[rr][threadIdx.x];
     bf16 dr[NDIGIT], di[NDIGIT];
     if (ex > EXP_ZERO) {
-      const double scale = ldexp(1.0, 7 - ex);
-      digits4(z.x, scale, dr);
-      digits4(z.y, scale, di);
+      digits4(z.x, ex, dr);
+      digits4(z.y, ex, di);
     } else {
 #pragma unroll
       for (int i = 0; i < NDIGIT; ++i) dr[i] = di[i] = __double2bfloat16(0.0);

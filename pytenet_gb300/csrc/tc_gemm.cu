@@ -19,9 +19,11 @@
 //     the row and column scales 2^(eA[m] + eB[n] - 14). Split-K partials are FP64.
 // What remains is the truncation of the fourth digit, ~2^-31 of the row maxima.
 //
-// Kernel: one 128 x 128 output tile per CTA (UMMA M=128, N=128, K=16), BK=64
-// (one 128-byte swizzle atom of BF16), 6-stage TMA -> shared memory pipeline with
-// full/empty mbarriers over (k block, digit pair) steps. Warp 0 lane 0 issues TMA,
+// Kernel: one 128 x 128 output tile per CTA (UMMA M=128, N=128, K=16), BK=32
+// (one 64-byte swizzle atom of BF16). A pipeline stage is one K block with all
+// four digit planes of both operands (two 3-D TMA boxes of 32 x 128 x 4, 64 KB),
+// so every plane is fetched once and feeds the 10 digit pairs x 2 MMAs of that
+// K block; 3 stages with full/empty mbarriers. Warp 0 lane 0 issues TMA,
 // warp 1 lane 0 issues tcgen05.mma and tcgen05.commit, warps 2..5 read the four
 // accumulators back with tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..) and write
 // FP64 complex results (or FP64 split-K partials). Every mbarrier wait is bounded:
@@ -41,17 +43,21 @@ void note_launches(int n);
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 64;
-constexpr int STAGES = 6;
+constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int STAGES = 3;
 constexpr int NDIGIT = 4;                 // digits per operand value
 constexpr int NPAIR = 10;                 // digit pairs (i, j) with i + j <= 3
 constexpr int NLEVEL = 4;
 // operand rows without a non-zero entry carry an exponent below this (the digit
 // converter fills the exponent arrays with 0x80 bytes before its max pass)
 constexpr int EXP_NONE = -2000;
-constexpr int A_TILE = BM * BK * 2;
+constexpr int A_TILE = BM * BK * 2;           // one digit plane of A: 8 KB
 constexpr int B_TILE = BN * BK * 2;
-constexpr int STAGE_BYTES = A_TILE + B_TILE;
+constexpr int A_STAGE = NDIGIT * A_TILE;       // all four planes
+constexpr int B_STAGE = NDIGIT * B_TILE;
+constexpr int STAGE_BYTES = A_STAGE + B_STAGE; // 64 KB
+// exact integer sums: at most this many real K entries per split
+constexpr int MAX_K_SPLIT = 2048;
 constexpr int THREADS = 192;
 constexpr int TMEM_COLS = NLEVEL * BN;   // 512: one accumulator per level
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
@@ -124,13 +130,14 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, in
       : "memory");
 }
 
-// shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+// shared-memory matrix descriptor: K-major, 64-byte swizzle (layout type 4), rows of
+// 64 B, 8-row groups 512 B apart
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
   d |= (uint64_t)1 << 16;
-  d |= (uint64_t)(1024 >> 4) << 32;
+  d |= (uint64_t)((8 * BK * 2) >> 4) << 32;
   d |= (uint64_t)1 << 46;
-  d |= (uint64_t)2 << 61;
+  d |= (uint64_t)4 << 61;
   return d;
 }
 
@@ -159,6 +166,26 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// sum_s 2^(8 (3 - s)) acc_s of four integer-valued FP32 level sums, times 2^sh.
+// Integer arithmetic throughout (the CUDA-core FP64 rate of this part is low): the
+// only FP64 operation is the int64 -> double conversion; the power of two goes
+// into the exponent field directly (ldexp only where that would leave the normal
+// range).
+__device__ __forceinline__ double combine_levels(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
+                                                 int sh) {
+  const long long i0 = __float2ll_rn(__uint_as_float(a0));
+  const long long i1 = __float2ll_rn(__uint_as_float(a1));
+  const long long i2 = __float2ll_rn(__uint_as_float(a2));
+  const long long i3 = __float2ll_rn(__uint_as_float(a3));
+  const long long v = ((i0 * 256 + i1) * 256 + i2) * 256 + i3;
+  if (v == 0) return 0.0;
+  const double r = (double)v;
+  const long long b = __double_as_longlong(r);
+  const int e = (int)((b >> 52) & 0x7FF) + sh;
+  if (e > 0 && e < 2047) return __longlong_as_double(b + ((long long)sh << 52));
+  return ldexp(r, sh);
+}
+
 __global__ void __launch_bounds__(THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const TcArgs p) {
@@ -167,7 +194,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
                                              ~uintptr_t(1023));
   uint8_t* sA = smem;
-  uint8_t* sB = smem + STAGES * A_TILE;
+  uint8_t* sB = smem + STAGES * A_STAGE;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
   uint64_t* tfull = empty + STAGES;
@@ -179,8 +206,8 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int split = blockIdx.z;
   const int kb0 = split * p.kb_per_split;
   const int kb1 = min(p.nkb, kb0 + p.kb_per_split);
-  // steps: k block outer, digit pair inner
-  const int it0 = kb0 * NPAIR, it1 = kb1 * NPAIR;
+  // one pipeline step per K block
+  const int it0 = kb0, it1 = kb1;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -217,10 +244,9 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       if (*(volatile int*)abort_flag) break;
-      const int kb = it / NPAIR, pr = it % NPAIR;
       mbar_expect_tx(&full[s], STAGE_BYTES);
-      tma_load_3d(sA + s * A_TILE, &tmA, kb * BK, m0, c_pair_a[pr], &full[s]);
-      tma_load_3d(sB + s * B_TILE, &tmB, kb * BK, n0, c_pair_b[pr], &full[s]);
+      tma_load_3d(sA + s * A_STAGE, &tmA, it * BK, m0, 0, &full[s]);
+      tma_load_3d(sB + s * B_STAGE, &tmB, it * BK, n0, 0, &full[s]);
       ++issued;
     }
     if (*(volatile int*)abort_flag) {
@@ -240,16 +266,19 @@ __global__ void __launch_bounds__(THREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int pr = it % NPAIR;
-      const uint32_t acc_col = (uint32_t)(c_pair_l[pr] * BN);
-      // the first k block of this split starts each level's accumulator
-      const bool first_of_level = (it / NPAIR == kb0) &&
-                                  (pr == 0 || c_pair_l[pr] != c_pair_l[pr - 1]);
-      const uint32_t a0 = smem_u32(sA + s * A_TILE), b0 = smem_u32(sB + s * B_TILE);
+      const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
 #pragma unroll
-      for (int k = 0; k < BK / 16; ++k)
-        umma(tmem + acc_col, sdesc(a0 + k * 32), sdesc(b0 + k * 32),
-             (first_of_level && k == 0) ? 0u : 1u);
+      for (int pr = 0; pr < NPAIR; ++pr) {
+        const uint32_t acc_col = (uint32_t)(c_pair_l[pr] * BN);
+        // the first k block of this split starts each level's accumulator
+        const bool first_of_level = (it == kb0) && (pr == 0 || c_pair_l[pr] != c_pair_l[pr - 1]);
+        const uint32_t ap = a0 + (uint32_t)(c_pair_a[pr] * A_TILE);
+        const uint32_t bp = b0 + (uint32_t)(c_pair_b[pr] * B_TILE);
+#pragma unroll
+        for (int k = 0; k < BK / 16; ++k)
+          umma(tmem + acc_col, sdesc(ap + k * 32), sdesc(bp + k * 32),
+               (first_of_level && k == 0) ? 0u : 1u);
+      }
       umma_commit(&empty[s]);
       ++issued;
     }
@@ -280,18 +309,11 @@ __global__ void __launch_bounds__(THREADS, 1)
           double re = 0.0, im = 0.0;
           const int eb = p.eb[col >> 1];
           if (have && ea > EXP_NONE && eb > EXP_NONE) {
-            // smallest level first; every FP32 -> FP64 conversion is exact
-            re = (double)__uint_as_float(v3[j]);
-            re = fma(re, 0x1p-8, (double)__uint_as_float(v2[j]));
-            re = fma(re, 0x1p-8, (double)__uint_as_float(v1[j]));
-            re = fma(re, 0x1p-8, (double)__uint_as_float(v0[j]));
-            im = (double)__uint_as_float(v3[j + 1]);
-            im = fma(im, 0x1p-8, (double)__uint_as_float(v2[j + 1]));
-            im = fma(im, 0x1p-8, (double)__uint_as_float(v1[j + 1]));
-            im = fma(im, 0x1p-8, (double)__uint_as_float(v0[j + 1]));
-            const double sc = ldexp(1.0, ea + eb - 14);
-            re *= sc;
-            im *= sc;
+            // value = (sum_s 2^(8 (3 - s)) acc_s) 2^(ea + eb - 38); the level sums are
+            // integer-valued FP32, combined exactly in int64, one rounding to FP64
+            const int sh = ea + eb - 38;
+            re = combine_levels(v0[j], v1[j], v2[j], v3[j], sh);
+            im = combine_levels(v0[j + 1], v1[j + 1], v2[j + 1], v3[j + 1], sh);
           }
           if (p.part != nullptr) {
             double2* dst = reinterpret_cast<double2*>(p.part + ((long)split * p.M + row) * p.N + col);
@@ -388,7 +410,8 @@ MapCache& map_cache() {
   return c;
 }
 
-// 3-D map over digit planes [4][rows][Kp] of BF16, logical extent (K, rows, 4), box (64, box_rows, 1)
+// 3-D map over digit planes [4][rows][Kp] of BF16, logical extent (K, rows, 4),
+// box (BK, box_rows, 4): one load brings a K block of all four planes
 bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, long plane,
               int box_rows) {
   MapKey key{ptr, rows, K, Kp, plane, box_rows};
@@ -405,11 +428,11 @@ bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, lon
   if (fn == nullptr) return false;
   cuuint64_t dims[3] = {(cuuint64_t)K, (cuuint64_t)rows, (cuuint64_t)NDIGIT};
   cuuint64_t strides[2] = {(cuuint64_t)Kp * 2, (cuuint64_t)plane * 2};
-  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, 1};
+  cuuint32_t box[3] = {(cuuint32_t)BK, (cuuint32_t)box_rows, (cuuint32_t)NDIGIT};
   cuuint32_t estr[3] = {1, 1, 1};
   CUtensorMap m;
   CUresult r = fn(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, const_cast<void*>(ptr), dims, strides,
-                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return false;
   std::lock_guard<std::mutex> lk(c.mu);
@@ -439,8 +462,9 @@ static int choose_splits(int M, int N, int nkb) {
   const int target = 2 * num_sms();
   int splits = 1;
   if (tiles < target) splits = std::max(1, std::min((target + tiles - 1) / tiles, nkb / 2));
-  // keep each split's exact integer sums short: at most 32 K blocks (2048 reals) per split
-  splits = std::max(splits, (nkb + 31) / 32);
+  // keep each split's exact integer sums short: at most MAX_K_SPLIT reals per split
+  constexpr int kb_max = MAX_K_SPLIT / BK;
+  splits = std::max(splits, (nkb + kb_max - 1) / kb_max);
   return std::min(splits, nkb);
 }
 

@@ -25,6 +25,8 @@ from .qnumber import is_qsparse, qnumber_flatten, qr_plan
 
 PREC = {"fp64": _lib.PREC_FP64, "plain": _lib.PREC_FP64, "mixed": _lib.PREC_SPLIT_BF16,
         "split-bf16": _lib.PREC_SPLIT_BF16}
+# smallest bond dimension (both sides) at which the mixed form uses the tensor cores
+MIXED_MIN_BOND = 64
 
 
 def prec_code(precision):
@@ -243,13 +245,24 @@ class Chain(DeviceMPS):
         for i in range(Lx):
             Dl, d, Dr = self.shape[i]
             cl, cr = self.chi[i], self.chi[i + 1]
-            need = max(need, L.ptn_site_step_workspace_bytes(Dl, d, Dr, cl, cr, self.prec),
-                       L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, self.prec),
-                       L.ptn_bond_step_workspace_bytes(Dr, Dr, cr, self.prec),
-                       L.ptn_bond_step_workspace_bytes(Dl, Dl, cl, self.prec))
+            for p in {self.prec, _lib.PREC_FP64}:
+                need = max(need, L.ptn_site_step_workspace_bytes(Dl, d, Dr, cl, cr, p),
+                           L.ptn_env_workspace_bytes(Dl, d, Dr, cl, cr, p),
+                           L.ptn_bond_step_workspace_bytes(Dr, Dr, cr, p),
+                           L.ptn_bond_step_workspace_bytes(Dl, Dl, cl, p))
         self.cws_bytes = need
         self.cws.get(need)
         self.depth = depth
+
+    def prec_for(self, Dl, Dr):
+        """Arithmetic of one local problem. The mixed form runs the tensor-core digit
+        GEMMs only where both bonds reach MIXED_MIN_BOND: below that the contractions
+        are too small to fill a 128 x 128 tile, and the Krylov space of a small
+        problem can be exhausted (a Lanczos breakdown at beta < 100 n eps), which
+        only the FP64 operator detects the way the reference does."""
+        if self.prec != _lib.PREC_FP64 and min(Dl, Dr) < MIXED_MIN_BOND:
+            return _lib.PREC_FP64
+        return self.prec
 
     # ---------------------------------------------------------------- envs
     def lview(self, i):
@@ -286,7 +299,8 @@ class Chain(DeviceMPS):
         a = self.buf[i]
         ws = self.cws.get(self.cws_bytes)
         call(L.ptn_env_step_left, ptr(a), ptr(a), ptr(self.w[i]), ptr(self.lenv[i]),
-             ptr(self.lenv[i + 1]), Dl, d, Dr, cl, cr, self.prec, ptr(ws), self.cws_bytes, st)
+             ptr(self.lenv[i + 1]), Dl, d, Dr, cl, cr, self.prec_for(Dl, Dr), ptr(ws),
+             self.cws_bytes, st)
         self.lshape[i + 1] = (Dr, cr, Dr)
 
     def env_right(self, i):
@@ -298,7 +312,8 @@ class Chain(DeviceMPS):
         a = self.buf[i]
         ws = self.cws.get(self.cws_bytes)
         call(L.ptn_env_step_right, ptr(a), ptr(a), ptr(self.w[i]), ptr(self.renv[i]),
-             ptr(self.renv[i - 1]), Dl, d, Dr, cl, cr, self.prec, ptr(ws), self.cws_bytes, st)
+             ptr(self.renv[i - 1]), Dl, d, Dr, cl, cr, self.prec_for(Dl, Dr), ptr(ws),
+             self.cws_bytes, st)
         self.rshape[i - 1] = (Dl, cl, Dl)
 
     # ---------------------------------------------------------------- local steps
@@ -308,15 +323,16 @@ class Chain(DeviceMPS):
         Dl, d, Dr = self.shape[i]
         cl, cr = self.chi[i], self.chi[i + 1]
         z = -complex(dt)
+        prec = self.prec_for(Dl, Dr)
         ws = self.cws.get(self.cws_bytes)
         if self.depth is not None:
             ctx = self.depth.ctx(i, 0)
             call(L.ptn_expm_site_ex, ptr(self.buf[i]), ptr(self.w[i]), ptr(self.lenv[i]),
-                 ptr(self.renv[i]), Dl, d, Dr, cl, cr, z.real, z.imag, self.numiter, self.prec,
+                 ptr(self.renv[i]), Dl, d, Dr, cl, cr, z.real, z.imag, self.numiter, prec,
                  _lib.C.byref(ctx), ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
             return
         call(L.ptn_expm_site, ptr(self.buf[i]), ptr(self.w[i]), ptr(self.lenv[i]),
-             ptr(self.renv[i]), Dl, d, Dr, cl, cr, z.real, z.imag, self.numiter, self.prec,
+             ptr(self.renv[i]), Dl, d, Dr, cl, cr, z.real, z.imag, self.numiter, prec,
              ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
 
     def bond_expm(self, c, l, r, chi, dt, site=0):
@@ -324,15 +340,16 @@ class Chain(DeviceMPS):
         L, st = lib(), stream_ptr()
         Dl, Dr = c.shape
         z = -complex(dt)
+        prec = self.prec_for(Dl, Dr)
         ws = self.cws.get(self.cws_bytes)
         if self.depth is not None:
             ctx = self.depth.ctx(site, 1)
             call(L.ptn_expm_bond_ex, ptr(c), ptr(l), ptr(r), Dl, Dr, chi, z.real, z.imag,
-                 self.numiter, self.prec, _lib.C.byref(ctx), ptr(self.V), ptr(self.state),
+                 self.numiter, prec, _lib.C.byref(ctx), ptr(self.V), ptr(self.state),
                  ptr(ws), self.cws_bytes, st)
             return
         call(L.ptn_expm_bond, ptr(c), ptr(l), ptr(r), Dl, Dr, chi, z.real, z.imag, self.numiter,
-             self.prec, ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
+             prec, ptr(self.V), ptr(self.state), ptr(ws), self.cws_bytes, st)
 
     def site_eigh(self, i):
         """Lowest Ritz vector of H_eff (_minimize_local_energy, dmrg.py:181-189)."""
@@ -341,7 +358,8 @@ class Chain(DeviceMPS):
         cl, cr = self.chi[i], self.chi[i + 1]
         ws = self.cws.get(self.cws_bytes)
         call(L.ptn_eigh_site, ptr(self.buf[i]), ptr(self.w[i]), ptr(self.lenv[i]),
-             ptr(self.renv[i]), Dl, d, Dr, cl, cr, self.numiter, self.prec, ptr(self.V),
+             ptr(self.renv[i]), Dl, d, Dr, cl, cr, self.numiter, self.prec_for(Dl, Dr),
+             ptr(self.V),
              ptr(self.state), ptr(ws), self.cws_bytes, st)
 
     # ---------------------------------------------------------------- sweeps

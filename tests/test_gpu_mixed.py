@@ -101,10 +101,30 @@ def test_mixed_contractions(ptg, dims):
                orc.apply_local_bond_contraction(c, lb, r)) < tol
 
 
+def tc_launches(fn):
+    """Run fn and count the tensor-core GEMM launches it made (kind 1 of the
+    library's profiling hooks)."""
+    import ctypes
+    import torch
+    from pytenet_gb300 import _lib
+    L = _lib.load()
+    torch.cuda.synchronize()
+    L.ptn_prof_start(1 << 1)
+    out = fn()
+    torch.cuda.synchronize()
+    L.ptn_prof_stop()
+    tot, fl, by, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+    _lib.check(L.ptn_prof_read(1, ctypes.byref(tot), ctypes.byref(fl), ctypes.byref(by),
+                               ctypes.byref(n)))
+    return out, n.value
+
+
 def test_mixed_tdvp_tracks_fp64(ptg):
-    """L=20, D=32 real time, 3 steps: mixed vs FP64 energy and fidelity."""
+    """L=20, D=128 real time, 3 steps: mixed vs FP64 energy and fidelity. Bonds of
+    64 and more run on the tensor cores (the mixed form keeps smaller local
+    problems in FP64)."""
     rng = np.random.default_rng(3)
-    L, D = 20, 32
+    L, D = 20, 128
     h = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 0.8, -0.1)
     h.zero_qnumbers()
     b = [min(2 ** min(i, L - i), D) for i in range(L + 1)]
@@ -115,28 +135,37 @@ def test_mixed_tdvp_tracks_fp64(ptg):
     pmx = ptg.MPS(psi.qsite, psi.qbonds, fill="postpone")
     pmx.a = [x.copy() for x in psi.a]
     ptg.tdvp_singlesite(h, p64, 0.05j, 3, numiter_lanczos=8, precision="fp64")
-    ptg.tdvp_singlesite(h, pmx, 0.05j, 3, numiter_lanczos=8, precision="mixed")
+    _, ntc = tc_launches(lambda: ptg.tdvp_singlesite(h, pmx, 0.05j, 3, numiter_lanczos=8,
+                                                     precision="mixed"))
+    assert ntc > 100
     e64 = orc.mpo_average(p64, h).real
     emx = orc.mpo_average(pmx, h).real
     ov = orc.mps_vdot(p64, pmx)
-    infid = 1 - abs(ov) ** 2 / (orc.mps_vdot(p64, p64).real * orc.mps_vdot(pmx, pmx).real)
-    print("energy rel err", abs(emx - e64) / abs(e64), "infidelity", infid)
-    assert abs(emx - e64) < 1e-10 * max(1.0, abs(e64))
-    assert infid < 1e-12
+    n64, nmx = orc.mps_vdot(p64, p64).real, orc.mps_vdot(pmx, pmx).real
+    infid = 1 - abs(ov) ** 2 / (n64 * nmx)
+    print("energy rel err", abs(emx - e64) / abs(e64), "infidelity", infid,
+          "norm drift", abs(np.sqrt(nmx) - np.sqrt(n64)), "tc launches", ntc)
+    # a random state's energy is close to zero, so the energy error is measured
+    # against the chain's energy scale L J (measured: ~5e-11 of it); the infidelity
+    # target of the mixed form is 1e-9
+    assert abs(emx - e64) < 1e-9 * L
+    assert infid < 1e-10
 
 
 def test_mixed_dmrg_energy(ptg):
     rng = np.random.default_rng(4)
-    L = 12
+    L = 16
     h = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 1.0, 0.0)
-    psi = ptg.MPS.construct_random(L, h.qsite, 0, max_vdim=24, dtype="complex", rng=rng)
+    psi = ptg.MPS.construct_random(L, h.qsite, 0, max_vdim=128, dtype="complex", rng=rng)
     p2 = ptg.MPS(psi.qsite, psi.qbonds, fill="postpone")
     p2.a = [x.copy() for x in psi.a]
     import warnings
     with warnings.catch_warnings():
         warnings.simplefilter("ignore")
         e64 = ptg.dmrg_singlesite(h, psi, 3, numiter_lanczos=20, precision="fp64")
-        emx = ptg.dmrg_singlesite(h, p2, 3, numiter_lanczos=20, precision="mixed")
-    print("dmrg energies", e64[-1], emx[-1])
+        emx, ntc = tc_launches(lambda: ptg.dmrg_singlesite(h, p2, 3, numiter_lanczos=20,
+                                                           precision="mixed"))
+    print("dmrg energies", e64[-1], emx[-1], "tc launches", ntc)
+    assert ntc > 100
     # the Ritz value is first-order in the ~4e-9 relative contraction error
     assert abs(emx[-1] - e64[-1]) < 1e-8 * abs(e64[-1])
