@@ -59,9 +59,15 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
     p.add_argument("--graph", action="store_true")
+    p.add_argument("--workload", default="xxz", choices=["xxz", "ising-batch"])
+    p.add_argument("--batch-count", type=int, default=256)
+    p.add_argument("--batch-seed", type=int, default=2027)
+    p.add_argument("--streams", type=int, default=None)
+    p.add_argument("--autotune", action="store_true")
+    p.add_argument("--cpu-instances", type=int, default=2)
     a = p.parse_args()
     if a.steps is None:
-        a.steps = 1 if a.form == "fp64" else 5
+        a.steps = 1 if (a.form == "fp64" or a.workload == "ising-batch") else 5
     assert a.warmup >= 3, "at least 3 warm-up steps"
     return a
 
@@ -369,6 +375,195 @@ def our_arm(a):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------ batch workload
+BATCH_METRIC = "TDVP site-updates/s, batch of 256 transverse-field Ising chains (L 16..48, D cap 32..256)"
+
+
+def batch_desc(a):
+    return (f"{a.batch_count} transverse-field Ising chains (seed {a.batch_seed}): J=1, "
+            f"g~U[0.5,1.5], h~U[0,0.2], L~U{{16..48}}, D cap from {{32,64,128,256}}, random product "
+            f"states embedded at the capped bonds; imaginary time dt=0.05, numiter_lanczos={a.m}; "
+            f"one step = sum over instances of (2L-1) site updates")
+
+
+def batch_cpu_sample(a, hs, psis, ninst):
+    """NumPy restatement of pytenet's tdvp_singlesite on all host cores for one
+    time step of `ninst` instances spread over the batch's cost range; the whole
+    batch's CPU time is extrapolated by the instances' cost (sum Dl Dr (Dl + Dr))."""
+    import copy
+    from oracle import ptn_oracle as orc
+    from pytenet_gb300.batch import instance_cost
+    costs = np.array([instance_cost(p) for p in psis])
+    order = np.argsort(costs)
+    # cheapest quartile: a sample that stays within seconds on the host
+    pick = [int(order[int(q * (len(order) - 1) * 0.25)]) for q in np.linspace(0.2, 1.0, ninst)]
+    secs, cost = 0.0, 0.0
+    import warnings
+    for i in pick:
+        p = copy.deepcopy(psis[i])
+        t0 = time.perf_counter()
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            orc.tdvp_singlesite(copy.deepcopy(hs[i]), p, 0.05, 1, a.m)
+        secs += time.perf_counter() - t0
+        cost += costs[i]
+    batch_sec = costs.sum() * secs / cost
+    site_updates = sum(2 * len(h.a) - 1 for h in hs)
+    sample = (f"one time step of {len(pick)} instances (L={[len(hs[i].a) for i in pick]}, "
+              f"{secs:.1f} s) of the NumPy restatement; batch time extrapolated by instance cost")
+    return site_updates / batch_sec, batch_sec, sample
+
+
+def batch_arm(a):
+    import torch
+    import __graft_entry__
+    __graft_entry__.build()
+    import pytenet_gb300 as ptg
+    from pytenet_gb300 import _lib, batch
+    L = _lib.load()
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    hs, psis, meta = batch.ising_batch(a.batch_count, a.batch_seed)
+    host0 = [[x.copy() for x in p.a] for p in psis]
+    prec = "fp64" if a.form == "fp64" else "mixed"
+    dt = 0.05
+    site_updates = sum(2 * len(h.a) - 1 for h in hs)
+    t_setup = time.perf_counter()
+    b = ptg.BatchTDVP(hs, psis, a.m, prec, streams=a.streams, autotune=a.autotune)
+    for _ in range(a.warmup):
+        b.step(dt)
+    torch.cuda.synchronize()
+    t_setup = time.perf_counter() - t_setup
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(a.steps):
+        b.step(dt)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    value = site_updates * a.steps / (ms / 1e3)
+    # kernel split and launch count from one eager step of every instance (graph
+    # replays bypass the host-side hooks)
+    import ctypes
+    launches0 = L.ptn_launch_count()
+    L.ptn_prof_start(0x1F)
+    torch.cuda.synchronize()
+    for r in b.runs:
+        r.chain.tdvp_step(dt)
+    torch.cuda.synchronize()
+    L.ptn_prof_stop()
+    prof_note = "one eager step of every instance, instance order; the library's hooks keep " \
+                "the first 32768 timed launches"
+    launches_step = L.ptn_launch_count() - launches0
+    kinds = {}
+    for k, name in enumerate(["zgemm_dmma (FP64 GEMM)", "tc_gemm (tcgen05 digit GEMM)",
+                              "mpo_stage", "qr", "krylov"]):
+        tot, fl, by, n = ctypes.c_double(), ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+        _lib.check(L.ptn_prof_read(k, ctypes.byref(tot), ctypes.byref(fl), ctypes.byref(by),
+                                   ctypes.byref(n)))
+        kinds[name] = {"ms": tot.value, "flops": fl.value, "bytes": by.value, "launches": n.value}
+    dom = "tc_gemm (tcgen05 digit GEMM)" if prec == "mixed" else "zgemm_dmma (FP64 GEMM)"
+    kd = kinds[dom]
+    achieved = kd["flops"] / (kd["ms"] / 1e3) / 1e12 if kd["ms"] > 0 else None
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    peak = peaks.get("bf16_tflops", 1900.0) if prec == "mixed" else 1.047
+    eager_total = sum(v["ms"] for v in kinds.values())
+    roofline = {"bound": "tensor", "kernel": dom, "achieved": achieved, "peak": peak,
+                "unit": "TFLOP/s", "frac": achieved / peak if achieved else None, "traffic": None,
+                "peak_source": ("bf16_tflops of measured" if prec == "mixed" else
+                                "FP64 DMMA m8n8k4 throughput measured on GB300 (1.047 TFLOP/s)"),
+                "measured_on": prof_note,
+                "kind_ms_eager_step": {k: v["ms"] for k, v in kinds.items()},
+                "kind_share_eager_step": {k: (v["ms"] / eager_total if eager_total else None)
+                                          for k, v in kinds.items()}}
+    # e2e through the public API: host MPS in and out, one step
+    e2e = None
+    if a.e2e_steps > 0:
+        pe = []
+        for p, t in zip(psis, host0):
+            q = ptg.MPS(p.qsite, p.qbonds, fill="postpone")
+            q.a = [x.copy() for x in t]
+            pe.append(q)
+        h2d = sum(x.nbytes for q in pe for x in q.a) + sum(
+            np.asarray(w, complex).nbytes for h in hs for w in h.a)
+        d2h = sum(x.nbytes for q in pe for x in q.a)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        import warnings
+        with warnings.catch_warnings():
+            warnings.simplefilter("ignore")
+            ptg.tdvp_singlesite_batch(hs, pe, dt, a.e2e_steps, a.m, prec, streams=b.nstreams,
+                                      graph=False, tuning=b.tuning)
+        torch.cuda.synchronize()
+        et = time.perf_counter() - t0
+        e2e = {"value": site_updates * a.e2e_steps / et, "unit": "site-updates/s",
+               "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+               "steps": a.e2e_steps,
+               "what": "tdvp_singlesite_batch(hs, psis_host, dt, numsteps) incl. uploads, "
+                       "right-normalisation, environments, download"}
+    cpu = None
+    if not a.no_cpu:
+        rate, bsec, sample = batch_cpu_sample(a, hs, [ptg_clone(ptg, p, t) for p, t in
+                                                     zip(psis, host0)], a.cpu_instances)
+        cpu = {"value": rate, "unit": "site-updates/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": sample}
+    dmix = {}
+    for m_ in meta:
+        dmix[m_["D"]] = dmix.get(m_["D"], 0) + 1
+    out = {"metric": BATCH_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": 1,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c128" if prec == "fp64" else "split-bf16 (fp32 acc) + fp64 krylov/qr",
+           "data": "synthetic",
+           "config": {"workload": batch_desc(a), "form": prec, "instances": a.batch_count,
+                      "site_updates_per_step": site_updates, "d_caps": dmix,
+                      "streams": b.nstreams, "autotune": bool(a.autotune), "graphs": True,
+                      "tuning": b.tuning, "setup_and_warmup_s": t_setup,
+                      "l2": "inputs larger than L2 (batch state of many GB)"},
+           "clocks": clk, "e2e": e2e, "gpu_launches": int(launches_step * a.steps),
+           "gpu_launches_note": "kernels per batch step counted on an eager step, times steps "
+                                "(the timed steps replay captured graphs of them)",
+           "roofline": roofline, "cpu_baseline": cpu}
+    print(json.dumps(out))
+
+
+def ptg_clone(ptg, p, tensors):
+    q = ptg.MPS(p.qsite, p.qbonds, fill="postpone")
+    q.a = [x.copy() for x in tensors]
+    return q
+
+
+def batch_reference_arm(a):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from pytenet_gb300 import batch
+    hs, psis, _ = batch.ising_batch(a.batch_count, a.batch_seed)
+    rates = []
+    for _ in range(a.steps):
+        rate, bsec, sample = batch_cpu_sample(a, hs, psis, a.cpu_instances)
+        rates.append(rate)
+    value = float(np.mean(rates))
+    site_updates = sum(2 * len(h.a) - 1 for h in hs)
+    out = {"metric": BATCH_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": a.gpus,
+           "steps": a.steps, "warmup": a.warmup, "ms_per_step": site_updates / value * 1e3,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
+           "data": "synthetic", "impl": "reference",
+           "config": {"workload": batch_desc(a)},
+           "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": os.cpu_count(),
+                            "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
 def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
     """Energy error, infidelity and norm drift of the benchmarked form (mixed, with
     the learned depth when given) against the plain FP64 fixed-depth form after
@@ -399,7 +594,12 @@ def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
 
 def main():
     a = parse()
-    if a.impl == "reference":
+    if a.workload == "ising-batch":
+        if a.impl == "reference":
+            batch_reference_arm(a)
+        else:
+            batch_arm(a)
+    elif a.impl == "reference":
         reference_arm(a)
     else:
         our_arm(a)

@@ -80,6 +80,26 @@ const char* ptn_version(void);
 const char* ptn_last_error(void);
 /* number of kernel launches issued by this library since load (diagnostics) */
 uint64_t ptn_launch_count(void);
+
+/* Tuning knobs (process-wide). They are read when an entry point chooses its
+ * launch shape on the host, so a CUDA graph keeps the values it was captured
+ * with; workspace queries read them too (query and call under the same values).
+ *   PTN_TUNE_TC_SPLIT_WAVES    split-K of the tensor-core GEMM aims at this many
+ *                              waves of CTAs (0..16, default 2; never fewer
+ *                              splits than exact integer accumulation needs)
+ *   PTN_TUNE_ZGEMM_SPLIT_WAVES split-K target of the FP64 GEMM (0..16, default 2;
+ *                              0 = no split-K)
+ *   PTN_TUNE_LARFB_TILE        QR block-update tile: 0 chosen per call (default),
+ *                              1 16x16, 2 32x16, 3 32x32, 4 64x32 (rows x columns)
+ * Used by the batched driver's autotuner (no reference counterpart). */
+enum {
+  PTN_TUNE_TC_SPLIT_WAVES = 0,
+  PTN_TUNE_ZGEMM_SPLIT_WAVES = 1,
+  PTN_TUNE_LARFB_TILE = 2,
+  PTN_TUNE_COUNT = 3
+};
+ptn_status ptn_tune_set(int key, int value);
+int ptn_tune_get(int key);
 /* Live kernel timing. ptn_prof_start(mask) clears the record and, for every
  * kind k with bit k set (0 FP64 GEMM, 1 tensor-core GEMM, 2 MPO stage, 3 QR,
  * 4 Krylov passes), brackets each launch with CUDA events on its stream (not

@@ -8,6 +8,9 @@ Drop-in API of the reference package (cmendl/pytenet) for this path:
     lanczos_iteration, expm_krylov, eigh_krylov, eigh_tridiag,
     block_sparse_qr and the quantum-number helpers,
     heisenberg_xxz_1d_mpo, ising_1d_mpo, mpo_average, mps_vdot, mps_norm.
+Additions: TDVPRun (device-resident run, optional CUDA graph), BatchTDVP /
+tdvp_singlesite_batch (many independent instances on streams), the mixed
+precision form (precision="mixed") and the learned Lanczos depth (learned.py).
 
 All numerics run in hand-written CUDA kernels for sm_103a (libptn_gb300.so,
 C ABI in include/pytenet_gb300.h). There is no CPU fallback: without the
@@ -27,6 +30,7 @@ from .chain_ops import (apply_local_hamiltonian, apply_local_bond_contraction,
 from .krylov import lanczos_iteration, expm_krylov, eigh_krylov, eigh_tridiag
 from .tdvp import tdvp_singlesite, TDVPRun
 from .dmrg import dmrg_singlesite
+from .batch import BatchTDVP, tdvp_singlesite_batch
 from ._lib import PtnError, PtnShapeError
 
 __version__ = "0.1.0"

@@ -17,6 +17,7 @@ KRYLOV_MAXITER = 64
 
 PTN_OK, PTN_BAD_SHAPE, PTN_BREAKDOWN, PTN_NAN, PTN_TIMEOUT, PTN_CUDA_ERROR, PTN_UNSUPPORTED = range(7)
 PREC_FP64, PREC_SPLIT_BF16 = 0, 1
+TUNE_TC_SPLIT_WAVES, TUNE_ZGEMM_SPLIT_WAVES, TUNE_LARFB_TILE = 0, 1, 2
 
 
 class PtnError(RuntimeError):
@@ -77,6 +78,8 @@ _SIGS = {
     "ptn_version": (C.c_char_p, []),
     "ptn_last_error": (C.c_char_p, []),
     "ptn_launch_count": (C.c_uint64, []),
+    "ptn_tune_set": (I, [I, I]),
+    "ptn_tune_get": (I, [I]),
     "ptn_prof_start": (None, [C.c_uint]),
     "ptn_prof_stop": (None, []),
     "ptn_prof_read": (I, [I, C.POINTER(D), C.POINTER(D), C.POINTER(D), C.POINTER(L)]),

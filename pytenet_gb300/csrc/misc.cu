@@ -23,6 +23,13 @@ void set_error(const char* fmt, ...) {
 
 void note_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
+namespace {
+std::atomic<int> g_tune[PTN_TUNE_COUNT] = {{2}, {2}, {0}};
+constexpr int kTuneMax[PTN_TUNE_COUNT] = {16, 16, 4};
+}  // namespace
+
+int tune(int key) { return (key >= 0 && key < PTN_TUNE_COUNT) ? g_tune[key].load() : 0; }
+
 int num_sms() {
   static int cached = 0;
   if (cached == 0) {
@@ -188,6 +195,17 @@ int ptn_abi_version(void) { return PTN_ABI_VERSION; }
 const char* ptn_version(void) { return "pytenet_gb300 0.1 (sm_103a)"; }
 const char* ptn_last_error(void) { return g_err; }
 uint64_t ptn_launch_count(void) { return g_launches.load(); }
+
+ptn_status ptn_tune_set(int key, int value) {
+  if (key < 0 || key >= PTN_TUNE_COUNT || value < 0 || value > kTuneMax[key]) {
+    set_error("ptn_tune_set: bad key %d or value %d", key, value);
+    return PTN_BAD_SHAPE;
+  }
+  g_tune[key].store(value);
+  return PTN_OK;
+}
+
+int ptn_tune_get(int key) { return tune(key); }
 
 void ptn_prof_start(unsigned kind_mask) {
   g_prof_used = 0;

@@ -42,6 +42,8 @@ void set_error(const char* fmt, ...);
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 int num_sms();
+// tuning knob value (ptn_tune_set); key is one of the PTN_TUNE_* constants
+int tune(int key);
 
 // ---------------------------------------------------------------------------
 // live kernel timing (off by default): launchers bracket a kernel of `kind`

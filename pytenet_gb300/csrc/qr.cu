@@ -940,6 +940,13 @@ ptn_status larfb_t(double2* C, long ldc, const double2* V, long ldv, int r0, int
 // launch enough CTAs to keep every SM's FP64 pipes busy
 ptn_status larfb(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
                  int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
+  switch (tune(PTN_TUNE_LARFB_TILE)) {
+    case 1: return larfb_t<16, 16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+    case 2: return larfb_t<32, 16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+    case 3: return larfb_t<32, 32>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+    case 4: return larfb_t<64, 32>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+    default: break;
+  }
   const long rows = m - r0;
   const long want = 2L * num_sms();
   auto ctas = [&](long rt, long ct) { return ((rows + rt - 1) / rt) * ((nc + ct - 1) / ct); };

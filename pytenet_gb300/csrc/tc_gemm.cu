@@ -459,7 +459,7 @@ int* err_flag() {
 
 static int choose_splits(int M, int N, int nkb) {
   const int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
-  const int target = 2 * num_sms();
+  const int target = tune(PTN_TUNE_TC_SPLIT_WAVES) * num_sms();
   int splits = 1;
   if (tiles < target) splits = std::max(1, std::min((target + tiles - 1) / tiles, nkb / 2));
   // keep each split's exact integer sums short: at most MAX_K_SPLIT reals per split
@@ -503,6 +503,10 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* 
   a.nkb = (K + BK - 1) / BK;
   const int gx = (N + BN - 1) / BN, gy = (M + BM - 1) / BM;
   int splits = choose_splits(M, N, a.nkb);
+  // a workspace sized under other knob values: fall back to fewer splits, but
+  // never below what exact integer accumulation needs
+  const int min_splits = (a.nkb + MAX_K_SPLIT / BK - 1) / (MAX_K_SPLIT / BK);
+  while (splits > min_splits && (size_t)splits * M * N * sizeof(double) > ws_bytes) --splits;
   if (splits > 1 && (size_t)splits * M * N * sizeof(double) > ws_bytes) {
     set_error("tc_gemm: workspace too small for %d K splits", splits);
     return PTN_BAD_SHAPE;

@@ -247,8 +247,9 @@ void launch_b(int ob, dim3 grid, cudaStream_t st, const KArgs& k) {
 int choose_splits(int M, int N, int K, int batch) {
   const long tiles = (long)((M + BM - 1) / BM) * ((N + BN - 1) / BN) * batch;
   const int sms = num_sms();
-  if (tiles >= sms || K < 8 * BK) return 1;
-  int s = (int)((2L * sms + tiles - 1) / tiles);
+  const int waves = tune(PTN_TUNE_ZGEMM_SPLIT_WAVES);
+  if (waves == 0 || tiles >= (long)waves * sms || K < 8 * BK) return 1;
+  int s = (int)(((long)waves * sms + tiles - 1) / tiles);
   s = std::min(s, K / (4 * BK));
   s = std::min(s, 32);
   return std::max(s, 1);

@@ -26,7 +26,7 @@ from .qnumber import is_qsparse, qnumber_flatten, qr_plan
 PREC = {"fp64": _lib.PREC_FP64, "plain": _lib.PREC_FP64, "mixed": _lib.PREC_SPLIT_BF16,
         "split-bf16": _lib.PREC_SPLIT_BF16}
 # smallest bond dimension (both sides) at which the mixed form uses the tensor cores
-MIXED_MIN_BOND = 64
+MIXED_MIN_BOND = 32
 
 
 def prec_code(precision):

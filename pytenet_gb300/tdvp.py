@@ -45,21 +45,20 @@ class TDVPRun:
     def _state_key(self):
         return ([q.tobytes() for q in self.chain.qbonds], list(self.chain.shape))
 
-    def step(self, dt):
-        """One symmetric time step exp(-dt H) (pytenet/tdvp.py:65-115)."""
-        if not self.use_graph:
-            self.chain.tdvp_step(dt)
-            self.steps_done += 1
-            return
+    def step(self, dt, capture=True):
+        """Exactly one symmetric time step exp(-dt H) (pytenet/tdvp.py:65-115).
+        With graph=True the first step runs eagerly and, if it left the integer
+        state (shapes, quantum numbers) unchanged, the same step is captured as a
+        CUDA graph -- capturing records without executing -- which later steps
+        with the same dt replay. capture=False skips the capture (a last step)."""
         if self.graph is not None and self.graph_dt == dt:
             self.graph.replay()
             self.steps_done += 1
             return
-        # eager step first; capture once the integer state no longer changes
         before = self._state_key()
         self.chain.tdvp_step(dt)
         self.steps_done += 1
-        if self._state_key() == before and self.steps_done >= 1:
+        if self.use_graph and capture and self._state_key() == before:
             torch.cuda.synchronize()
             g = torch.cuda.CUDAGraph()
             s = torch.cuda.Stream()
@@ -71,9 +70,6 @@ class TDVPRun:
             assert self._state_key() == before
             self.graph = g
             self.graph_dt = dt
-            # the captured step did not execute; run it now
-            g.replay()
-            self.steps_done += 1
 
     def download(self):
         self.chain.download(self.psi)
@@ -86,15 +82,8 @@ def tdvp_singlesite(hamiltonian, psi, dt, numsteps, numiter_lanczos=25, precisio
     state and the norm of the initial `psi` is returned (pytenet/tdvp.py:26-118).
     All numerics run on the GPU."""
     run = TDVPRun(hamiltonian, psi, numiter_lanczos, precision, graph, depth_model, depth_tol)
-    done = 0
-    while done < numsteps:
-        before = run.steps_done
-        if graph and run.graph is None and numsteps - done == 1:
-            run.chain.tdvp_step(dt)
-            run.steps_done += 1
-        else:
-            run.step(dt)
-        done += run.steps_done - before
+    for n in range(numsteps):
+        run.step(dt, capture=(n < numsteps - 1))
     run.download()
     warn_breakdowns(run.chain)
     return float(run.nrm.item())

@@ -121,7 +121,7 @@ def tc_launches(fn):
 
 def test_mixed_tdvp_tracks_fp64(ptg):
     """L=20, D=128 real time, 3 steps: mixed vs FP64 energy and fidelity. Bonds of
-    64 and more run on the tensor cores (the mixed form keeps smaller local
+    32 and more run on the tensor cores (the mixed form keeps smaller local
     problems in FP64)."""
     rng = np.random.default_rng(3)
     L, D = 20, 128
