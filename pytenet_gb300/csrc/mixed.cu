@@ -39,7 +39,7 @@ ptn_status mpo_stage_f64(const double2* in, double2* out, const double2* w, long
 namespace {
 
 typedef __nv_bfloat16 bf16;
-constexpr int NDIGIT = 4;
+constexpr int NDIGIT = 5;
 constexpr int EXP_ZERO = -2000;   // rows with no non-zero entry (memset 0x80 gives less)
 
 // 32 x 32 complex tile of the view, rows r0.., cols k0..; threads (32, 8)
@@ -89,18 +89,19 @@ __global__ void rowexp_kernel(const double2* __restrict__ src, long sr, long sk,
 }
 
 // Balanced base-256 digits of x 2^(7 - ex) (|x| < 2^ex): the fixed-point integer
-// T = round(x 2^(31 - ex)) (|T| <= 2^31) is cut into T = d0 2^24 + d1 2^16 + d2 2^8 + d3
-// with d1..d3 in [-128, 127] and |d0| <= 128, each exact in BF16. Integer
+// T = round(x 2^(39 - ex)) (|T| <= 2^39) is cut into
+// T = d0 2^32 + d1 2^24 + d2 2^16 + d3 2^8 + d4 with d1..d4 in [-128, 127] and
+// |d0| <= 128, each exact in BF16. Integer
 // arithmetic on the IEEE fields only: the CUDA-core FP64 rate of this part is low.
 // Zero and subnormal entries (below 2^-1022) give zero digits.
-__device__ __forceinline__ void digits4(double x, int ex, bf16 (&d)[NDIGIT]) {
+__device__ __forceinline__ void digits_of(double x, int ex, bf16 (&d)[NDIGIT]) {
   const long long b = __double_as_longlong(x);
   const int E = (int)((b >> 52) & 0x7FF);
   long long T = 0;
   if (E != 0) {
     const long long mant = (b & ((1LL << 52) - 1)) | (1LL << 52);
-    // x = mant 2^(E - 1075): T = round(mant 2^(E - 1075 + 31 - ex)), shift always right
-    const int rs = 1075 - 31 + ex - E;
+    // x = mant 2^(E - 1075): T = round(mant 2^(E - 1075 + 39 - ex)), shift always right
+    const int rs = 1075 - (8 * NDIGIT - 1) + ex - E;
     if (rs < 63) T = (rs <= 0) ? (mant << (-rs)) : ((mant + (1LL << (rs - 1))) >> rs);
     if (b < 0) T = -T;
   }
@@ -130,8 +131,8 @@ __global__ void digits_kernel(const double2* __restrict__ src, long sr, long sk,
     const double2 z = tile[rr][threadIdx.x];
     bf16 dr[NDIGIT], di[NDIGIT];
     if (ex > EXP_ZERO) {
-      digits4(z.x, ex, dr);
-      digits4(z.y, ex, di);
+      digits_of(z.x, ex, dr);
+      digits_of(z.y, ex, di);
     } else {
 #pragma unroll
       for (int i = 0; i < NDIGIT; ++i) dr[i] = di[i] = __double2bfloat16(0.0);

@@ -33,8 +33,6 @@ namespace {
 
 constexpr int NB = 16;     // panel width
 constexpr int PT = 512;    // panel kernel threads
-constexpr int RT = 64;     // rows per block-update tile
-constexpr int CTL = 32;    // columns per block-update tile
 
 __device__ __forceinline__ double2 crecip(double2 a) {
   const double s = 1.0 / (a.x * a.x + a.y * a.y);
@@ -627,6 +625,14 @@ __device__ __forceinline__ int rs_index(int lane) {
   return ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
 }
 
+// Panel on a cluster, one row per thread, 1..QW warps per CTA (as many as the row
+// chunk needs: idle warps would spend the scarce FP64 issue slots on zeros). The
+// CTA's rows live in shared memory column-major (xs[c][thread]: conflict-free)
+// and the column loop stays rolled, so one small loop body serves every column
+// (a fully unrolled body stalled on instruction fetch). Per column: the norm
+// (one cluster barrier, partials read through DSMEM), the reflector, one
+// reduce-scatter of w_c = v^H a_c (c > jj) and of the Gram column g_p = v_p^H v
+// (p < jj) (second barrier), the rank-1 update of the remaining panel columns.
 __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict__ a, long lda, int m,
                                                             int j0, int jb,
                                                             double2* __restrict__ Tout,
@@ -635,12 +641,15 @@ __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict_
   const int rank = (int)cluster.block_rank();
   const int cs = (int)cluster.num_blocks();
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = (int)(blockDim.x >> 5);
+  __shared__ double2 xs[NB][QW * 32];     // this CTA's panel rows, column-major
   __shared__ double s_wn[QW];             // per-warp norm partials
-  __shared__ double2 s_wv[QW][2 * NB];    // per-warp vector partials (w and g)
+  __shared__ double2 s_wv[QW][NB];        // per-warp vector partials
   __shared__ double s_nrm;                // CTA partial norm (read remotely)
   __shared__ double2 s_alpha;
-  __shared__ double2 s_vec[2 * NB];       // CTA partial vectors (read remotely)
-  __shared__ double2 s_G[NB][NB];         // summed Gram (rank 0)
+  __shared__ double2 s_vec[NB];           // CTA partial vectors (read remotely)
+  __shared__ double2 s_tau[NB];
+  __shared__ double2 s_G[NB][NB];         // Gram entries v_p^H v_c, p < c (rank 0)
 
   const int mp = m - j0;
   const int chunk = (mp + cs - 1) / cs;
@@ -649,89 +658,93 @@ __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict_
   const int i = rb + tid;                 // this thread's row
   const bool mine = i < re;
 
-  double2 x[NB];
 #pragma unroll
-  for (int c = 0; c < NB; ++c) x[c] = (mine && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
-  double2 taus_l[NB];
-  double2 Gcol[NB];   // rank 0: G[p][c] for this thread's p = tid, filled per column c
+  for (int c = 0; c < NB; ++c) xs[c][tid] = (mine && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
+  for (int e = tid; e < NB * NB; e += blockDim.x) s_G[e / NB][e % NB] = c2(0.0, 0.0);
 
+#pragma unroll 1
+  for (int jj = 0; jj < jb; ++jj) {
+    const int col = j0 + jj;
+    const int owner = jj / chunk;
+    // ---- norm of the part below the diagonal
+    const double2 xj = xs[jj][tid];
+    double acc = (mine && i > col) ? fma(xj.x, xj.x, xj.y * xj.y) : 0.0;
 #pragma unroll
-  for (int jj = 0; jj < NB; ++jj) {
-    if (jj < jb) {
-      const int col = j0 + jj;
-      const int owner = jj / chunk;
-      // ---- norm
-      double acc = (mine && i > col) ? fma(x[jj].x, x[jj].x, x[jj].y * x[jj].y) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_wn[warp] = acc;
+    if (i == col) s_alpha = xj;
+    __syncthreads();
+    if (tid == 0) {
+      const double h0 = s_wn[0] + ((nw > 1) ? s_wn[1] : 0.0);
+      const double h1 = (nw > 2) ? s_wn[2] + ((nw > 3) ? s_wn[3] : 0.0) : 0.0;
+      s_nrm = h0 + h1;
+    }
+    cluster.sync();
+    double v = (lane < cs) ? *cluster.map_shared_rank(&s_nrm, lane) : 0.0;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-      if (lane == 0) s_wn[warp] = acc;
-      if (i == col) s_alpha = x[jj];
-      __syncthreads();
-      if (tid == 0) s_nrm = (s_wn[0] + s_wn[1]) + (s_wn[2] + s_wn[3]);
-      cluster.sync();
-      double v = (lane < cs) ? *cluster.map_shared_rank(&s_nrm, lane) : 0.0;
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const double xn2 = v;
+    const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
+    double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
+    double beta = 0.0;
+    const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
+    if (apply) {
+      beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+      const double ib = 1.0 / beta;
+      tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
+      scal = crecip(c2(alpha.x - beta, alpha.y));
+    }
+    if (tid == 0) s_tau[jj] = tau;
+    double2 xjn = xj;
+    if (apply && mine && i > col) xjn = cmul(xj, scal);
+    if (apply && i == col) xjn = c2(beta, 0.0);
+    xs[jj][tid] = xjn;
+    // ---- one reduction: w_c = v^H a_c (c > jj) and g_p = v_p^H v (p < jj)
+    const double2 vcur = (mine && i >= col) ? ((i == col) ? c2(1.0, 0.0) : xjn) : c2(0.0, 0.0);
+    double2 q[NB];
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      const double xn2 = v;
-      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
-      double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
-      double beta = 0.0;
-      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
-      if (apply) {
-        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
-        const double ib = 1.0 / beta;
-        tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
-        scal = crecip(c2(alpha.x - beta, alpha.y));
+    for (int c = 0; c < NB; ++c) {
+      const double2 xc = xs[c][tid];
+      if (c > jj) {
+        q[c] = cmul(cconj(vcur), xc);
+      } else if (c < jj) {
+        const double2 vp = (mine && i >= j0 + c) ? ((i == j0 + c) ? c2(1.0, 0.0) : xc) : c2(0.0, 0.0);
+        q[c] = cmul(cconj(vp), vcur);
+      } else {
+        q[c] = c2(0.0, 0.0);
       }
-      taus_l[jj] = tau;
-      if (apply && mine && i > col) x[jj] = cmul(x[jj], scal);
-      if (apply && i == col) x[jj] = c2(beta, 0.0);
-      // ---- one reduction: w_c = v^H a_c (c > jj) and g_p = v_p^H v (p < jj)
-      const double2 vcur = (mine && i >= col) ? ((i == col) ? c2(1.0, 0.0) : x[jj]) : c2(0.0, 0.0);
-      double2 q[NB];
+    }
+    const double2 ws = reduce_scatter16(q, lane);
+    const int qi = rs_index(lane);
+    if ((lane & 1) == 0) s_wv[warp][qi] = ws;
+    __syncthreads();
+    if (tid < NB) {
+      const double2 h0 = (nw > 1) ? cadd(s_wv[0][tid], s_wv[1][tid]) : s_wv[0][tid];
+      const double2 h1 = (nw > 2) ? ((nw > 3) ? cadd(s_wv[2][tid], s_wv[3][tid]) : s_wv[2][tid])
+                                  : c2(0.0, 0.0);
+      s_vec[tid] = (nw > 2) ? cadd(h0, h1) : h0;
+    }
+    cluster.sync();
+    // ---- gather: lane c (< NB) of every warp sums rank by rank (tree, same order everywhere)
+    double2 tot = c2(0.0, 0.0);
+    if (lane < NB) {
+      double2 vals[16];
 #pragma unroll
-      for (int c = 0; c < NB; ++c) {
-        if (c > jj) q[c] = cmul(cconj(vcur), x[c]);
-        else if (c < jj) {
-          const double2 vp = (mine && i >= j0 + c) ? ((i == j0 + c) ? c2(1.0, 0.0) : x[c]) : c2(0.0, 0.0);
-          q[c] = cmul(cconj(vp), vcur);
-        } else q[c] = c2(0.0, 0.0);
-      }
-      const double2 ws = reduce_scatter16(q, lane);
-      const int qi = rs_index(lane);
-      if ((lane & 1) == 0) s_wv[warp][qi] = ws;
-      __syncthreads();
-      if (tid < NB)
-        s_vec[tid] = cadd(cadd(s_wv[0][tid], s_wv[1][tid]), cadd(s_wv[2][tid], s_wv[3][tid]));
-      cluster.sync();
-      // ---- gather: lane c (< NB) of every warp sums rank by rank (tree, same order everywhere)
-      double2 tot = c2(0.0, 0.0);
-      if (lane < NB) {
-        double2 vals[16];
+      for (int r = 0; r < 16; ++r)
+        vals[r] = (r < cs) ? cluster.map_shared_rank(s_vec, r)[lane] : c2(0.0, 0.0);
 #pragma unroll
-        for (int r = 0; r < 16; ++r)
-          vals[r] = (r < cs) ? cluster.map_shared_rank(s_vec, r)[lane] : c2(0.0, 0.0);
+      for (int h = 8; h > 0; h >>= 1)
 #pragma unroll
-        for (int h = 8; h > 0; h >>= 1)
+        for (int r = 0; r < h; ++r) vals[r] = cadd(vals[r], vals[r + h]);
+      tot = vals[0];
+    }
+    if (rank == 0 && warp == 0 && lane < jj) s_G[lane][jj] = tot;
+    // ---- rank-1 update of this thread's row
+    const double2 ctau = cconj(tau);
 #pragma unroll
-          for (int r = 0; r < h; ++r) vals[r] = cadd(vals[r], vals[r + h]);
-        tot = vals[0];
-      }
-      // Gram column jj for T (only rank 0 needs it): thread p keeps G[p][jj]
-      {
-        const double2 gp = c2(__shfl_sync(0xffffffffu, tot.x, lane & 15),
-                              __shfl_sync(0xffffffffu, tot.y, lane & 15));
-        if (tid < jj) Gcol[jj] = gp;
-      }
-      // ---- rank-1 update of this thread's row
-      const double2 ctau = cconj(tau);
-#pragma unroll
-      for (int c = 0; c < NB; ++c) {
-        if (c > jj) {
-          const double2 wcc = c2(__shfl_sync(0xffffffffu, tot.x, c), __shfl_sync(0xffffffffu, tot.y, c));
-          if (apply && mine && i >= col) x[c] = csub(x[c], cmul(vcur, cmul(ctau, wcc)));
-        }
-      }
+    for (int c = 0; c < NB; ++c) {
+      const double2 wcc = c2(__shfl_sync(0xffffffffu, tot.x, c), __shfl_sync(0xffffffffu, tot.y, c));
+      if (c > jj && apply && mine && i >= col) xs[c][tid] = csub(xs[c][tid], cmul(vcur, cmul(ctau, wcc)));
     }
   }
 
@@ -741,17 +754,14 @@ __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict_
     for (int c = 0; c < NB; ++c) {
       if (c < jb) {
         const int col = j0 + c;
-        a[(long)i * lda + col] = x[c];
-        V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x[c];
+        const double2 x = xs[c][tid];
+        a[(long)i * lda + col] = x;
+        V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x;
       }
     }
   }
-  // ---- T (zlarft) on rank 0 from the Gram columns kept by threads p < NB
+  // ---- T (zlarft) on rank 0 from the Gram entries
   if (rank == 0) {
-    if (tid < NB) {
-#pragma unroll
-      for (int c = 0; c < NB; ++c) s_G[tid][c] = (tid < c && c < jb) ? Gcol[c] : c2(0.0, 0.0);
-    }
     __syncthreads();
     if (warp == 0) {
       double2 T[NB];   // lane p holds row p of T
@@ -764,7 +774,7 @@ __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict_
 #pragma unroll
           for (int qq = 0; qq < NB; ++qq)
             if (qq < c && lane <= qq) acc2 = cfma(T[qq], s_G[qq][c], acc2);
-          const double2 tc = taus_l[c];
+          const double2 tc = s_tau[c];
           if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc2);
           if (lane == c) T[c] = tc;
         }
@@ -827,25 +837,14 @@ __global__ void __launch_bounds__(256) larfb_partial_kernel(const double2* __res
   }
 }
 
-// W = sum_rb partial; W2 = op(T) W (op = T^H if conjT else T); C -= V W2 on this tile
-template <int RTT, int CTT>
-__global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__ C, long ldc,
-                                                           const double2* __restrict__ V, long ldv,
-                                                           int r0, int m, int c0, int nc, int v0,
-                                                           int jb, const double2* __restrict__ part,
-                                                           int nrb, const double2* __restrict__ T,
-                                                           int conjT) {
-  __shared__ double2 sv[RTT][NB];
+// W = sum_rb partial; W2 = op(T) W (op = T^H if conjT else T), once per column
+// tile; W2 overwrites block 0 of the partials (each CTA owns its columns).
+template <int CTT>
+__global__ void __launch_bounds__(256) larfb_w2_kernel(double2* __restrict__ part, int nc, int jb,
+                                                       int nrb, const double2* __restrict__ T,
+                                                       int conjT) {
   __shared__ double2 sw[NB][CTT];
-  __shared__ double2 sw2[NB][CTT];
   __shared__ double2 sT[NB][NB];
-  const int rb = blockIdx.y;
-  const int rbase = r0 + rb * RTT;
-  for (int idx = threadIdx.x; idx < RTT * NB; idx += blockDim.x) {
-    const int rr = idx / NB, j = idx % NB;
-    const int r = rbase + rr;
-    sv[rr][j] = (r < m && j < jb) ? V[(long)r * ldv + v0 + j] : c2(0.0, 0.0);
-  }
   if (threadIdx.x < NB * NB) sT[threadIdx.x / NB][threadIdx.x % NB] = T[threadIdx.x];
   for (int idx = threadIdx.x; idx < NB * CTT; idx += blockDim.x) {
     const int j = idx / CTT, cc = idx % CTT;
@@ -858,6 +857,7 @@ __global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__
   __syncthreads();
   for (int idx = threadIdx.x; idx < NB * CTT; idx += blockDim.x) {
     const int j = idx / CTT, cc = idx % CTT;
+    const int c = blockIdx.x * CTT + cc;
     double2 s = c2(0.0, 0.0);
     if (j < jb) {
       if (conjT) {
@@ -866,7 +866,29 @@ __global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__
         for (int q = j; q < jb; ++q) s = cadd(s, cmul(sT[j][q], sw[q][cc]));
       }
     }
-    sw2[j][cc] = s;
+    if (c < nc) part[(long)j * nc + c] = s;
+  }
+}
+
+// C -= V W2 on this tile (W2 from larfb_w2_kernel)
+template <int RTT, int CTT>
+__global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__ C, long ldc,
+                                                           const double2* __restrict__ V, long ldv,
+                                                           int r0, int m, int c0, int nc, int v0,
+                                                           int jb, const double2* __restrict__ W2) {
+  __shared__ double2 sv[RTT][NB];
+  __shared__ double2 sw2[NB][CTT];
+  const int rb = blockIdx.y;
+  const int rbase = r0 + rb * RTT;
+  for (int idx = threadIdx.x; idx < RTT * NB; idx += blockDim.x) {
+    const int rr = idx / NB, j = idx % NB;
+    const int r = rbase + rr;
+    sv[rr][j] = (r < m && j < jb) ? V[(long)r * ldv + v0 + j] : c2(0.0, 0.0);
+  }
+  for (int idx = threadIdx.x; idx < NB * CTT; idx += blockDim.x) {
+    const int j = idx / CTT, cc = idx % CTT;
+    const int c = blockIdx.x * CTT + cc;
+    sw2[j][cc] = (j < jb && c < nc) ? W2[(long)j * nc + c] : c2(0.0, 0.0);
   }
   __syncthreads();
   const int tc = threadIdx.x % CTT, tr = threadIdx.x / CTT;
@@ -929,10 +951,10 @@ ptn_status larfb_t(double2* C, long ldc, const double2* V, long ldv, int r0, int
   const int nrb = (m - r0 + RTT - 1) / RTT;
   dim3 grid((nc + CTT - 1) / CTT, nrb);
   larfb_partial_kernel<RTT, CTT><<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part);
-  larfb_update_kernel<RTT, CTT><<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part,
-                                                      nrb, T, conjT ? 1 : 0);
+  larfb_w2_kernel<CTT><<<grid.x, 256, 0, st>>>(part, nc, jb, nrb, T, conjT ? 1 : 0);
+  larfb_update_kernel<RTT, CTT><<<grid, 256, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part);
   PTN_LAUNCH_CHECK();
-  note_launches(2);
+  note_launches(3);
   return PTN_OK;
 }
 
@@ -1027,7 +1049,7 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
     if (cs > 1 && chunk <= QW * 32) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs);
-      cfg.blockDim = dim3(QW * 32);
+      cfg.blockDim = dim3(32 * ((chunk + 31) / 32));   // warps the row chunk needs
       cfg.dynamicSmemBytes = 0;
       cfg.stream = st;
       cudaLaunchAttribute attr[1];

@@ -8,22 +8,24 @@
 //     (2N x 2K, K-major), so that the real product (M x 2N) is the complex
 //     product with re/im interleaved -- i.e. the complex128 output layout;
 //   - every operand row r is scaled by its own power of two 2^-e[r] (|x| < 2^e[r]
-//     over the row) and cut into four signed 8-bit integer digits held exactly in
+//     over the row) and cut into five signed 8-bit integer digits held exactly in
 //     BF16: x = 2^(e[r]-7) * sum_i 2^(-8 i) d_i, |d_i| <= 128 (Ozaki, Ogita, Oishi
 //     and Rump's error-free splitting, in fixed point per row);
 //   - a digit product is an integer of at most 14 bits, so the products of one
-//     level s = i + j (pairs with s <= 3, ten in all) add up exactly in an FP32
-//     accumulator as long as the partial sums stay below 2^24; each level has its
-//     own accumulator in tensor memory (4 levels x 128 columns = all 512 columns);
-//   - the epilogue combines the levels in FP64, sum_s 2^(-8 s) acc_s, and applies
-//     the row and column scales 2^(eA[m] + eB[n] - 14). Split-K partials are FP64.
-// What remains is the truncation of the fourth digit, ~2^-31 of the row maxima.
+//     level s = i + j (pairs with s <= 4, fifteen in all) add up exactly in an
+//     FP32 accumulator while the partial sums stay below 2^24 (K per split is
+//     capped); each level has its own accumulator in tensor memory (5 levels x 96
+//     columns of the 512);
+//   - the epilogue combines the levels exactly in integer arithmetic and applies
+//     the row and column scales 2^(eA[m] + eB[n] - 46). Split-K partials are FP64.
+// What remains is the truncation after the fifth digit and the dropped level-5
+// products, ~2^-39 of the row maxima: FP64-class for the sweep's purposes.
 //
-// Kernel: one 128 x 128 output tile per CTA (UMMA M=128, N=128, K=16), BK=32
+// Kernel: one 128 x 96 output tile per CTA (UMMA M=128, N=96, K=16), BK=32
 // (one 64-byte swizzle atom of BF16). A pipeline stage is one K block with all
-// four digit planes of both operands (two 3-D TMA boxes of 32 x 128 x 4, 64 KB),
-// so every plane is fetched once and feeds the 10 digit pairs x 2 MMAs of that
-// K block; 3 stages with full/empty mbarriers. Warp 0 lane 0 issues TMA,
+// five digit planes of both operands (3-D TMA boxes of 32 x 128 x 5 and
+// 32 x 96 x 5, 70 KB), so every plane is fetched once and feeds the 15 digit
+// pairs x 2 MMAs of that K block; 3 stages with full/empty mbarriers. Warp 0 lane 0 issues TMA,
 // warp 1 lane 0 issues tcgen05.mma and tcgen05.commit, warps 2..5 read the four
 // accumulators back with tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..) and write
 // FP64 complex results (or FP64 split-K partials). Every mbarrier wait is bounded:
@@ -43,30 +45,32 @@ void note_launches(int n);
 
 namespace {
 
-constexpr int BM = 128, BN = 128, BK = 32;
+constexpr int BM = 128, BN = 96, BK = 32;
 constexpr int STAGES = 3;
-constexpr int NDIGIT = 4;                 // digits per operand value
-constexpr int NPAIR = 10;                 // digit pairs (i, j) with i + j <= 3
-constexpr int NLEVEL = 4;
+constexpr int NDIGIT = 5;                 // digits per operand value
+constexpr int NPAIR = 15;                 // digit pairs (i, j) with i + j <= 4
+constexpr int NLEVEL = 5;
 // operand rows without a non-zero entry carry an exponent below this (the digit
 // converter fills the exponent arrays with 0x80 bytes before its max pass)
 constexpr int EXP_NONE = -2000;
 constexpr int A_TILE = BM * BK * 2;           // one digit plane of A: 8 KB
 constexpr int B_TILE = BN * BK * 2;
-constexpr int A_STAGE = NDIGIT * A_TILE;       // all four planes
+constexpr int A_STAGE = NDIGIT * A_TILE;       // all five planes
 constexpr int B_STAGE = NDIGIT * B_TILE;
-constexpr int STAGE_BYTES = A_STAGE + B_STAGE; // 64 KB
+constexpr int STAGE_BYTES = A_STAGE + B_STAGE; // 70 KB
 // exact integer sums: at most this many real K entries per split
 constexpr int MAX_K_SPLIT = 2048;
 constexpr int THREADS = 192;
-constexpr int TMEM_COLS = NLEVEL * BN;   // 512: one accumulator per level
+constexpr int TMEM_USED = NLEVEL * BN;   // 480: one accumulator per level
+constexpr int TMEM_COLS = 512;           // allocation (a power of two)
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr long WAIT_LIMIT = 1L << 22;
 // kind::f16 instruction descriptor: FP32 accumulate (bit 4), A and B BF16
 // (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
 constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
                            ((uint32_t)(BM >> 4) << 24);
-static_assert(TMEM_COLS <= 512, "tensor memory holds 512 columns");
+static_assert(TMEM_USED <= TMEM_COLS, "tensor memory holds 512 columns");
+static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
 
 struct TcArgs {
   int M, N;            // output rows, real output columns (2 x complex columns)
@@ -83,9 +87,9 @@ struct TcArgs {
 };
 
 // digit pairs, grouped by level; the first pair of each level starts its accumulator
-__constant__ int c_pair_a[NPAIR] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3};
-__constant__ int c_pair_b[NPAIR] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0};
-__constant__ int c_pair_l[NPAIR] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3};
+__constant__ int c_pair_a[NPAIR] = {0, 0, 1, 0, 1, 2, 0, 1, 2, 3, 0, 1, 2, 3, 4};
+__constant__ int c_pair_b[NPAIR] = {0, 1, 0, 2, 1, 0, 3, 2, 1, 0, 4, 3, 2, 1, 0};
+__constant__ int c_pair_l[NPAIR] = {0, 1, 1, 2, 2, 2, 3, 3, 3, 3, 4, 4, 4, 4, 4};
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return static_cast<uint32_t>(__cvta_generic_to_shared(p));
@@ -166,18 +170,19 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
-// sum_s 2^(8 (3 - s)) acc_s of four integer-valued FP32 level sums, times 2^sh.
+// sum_s 2^(8 (4 - s)) acc_s of five integer-valued FP32 level sums, times 2^sh.
 // Integer arithmetic throughout (the CUDA-core FP64 rate of this part is low): the
 // only FP64 operation is the int64 -> double conversion; the power of two goes
 // into the exponent field directly (ldexp only where that would leave the normal
 // range).
 __device__ __forceinline__ double combine_levels(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                                 int sh) {
+                                                 uint32_t a4, int sh) {
   const long long i0 = __float2ll_rn(__uint_as_float(a0));
   const long long i1 = __float2ll_rn(__uint_as_float(a1));
   const long long i2 = __float2ll_rn(__uint_as_float(a2));
   const long long i3 = __float2ll_rn(__uint_as_float(a3));
-  const long long v = ((i0 * 256 + i1) * 256 + i2) * 256 + i3;
+  const long long i4 = __float2ll_rn(__uint_as_float(a4));
+  const long long v = (((i0 * 256 + i1) * 256 + i2) * 256 + i3) * 256 + i4;   // |v| < 2^58
   if (v == 0) return 0.0;
   const double r = (double)v;
   const long long b = __double_as_longlong(r);
@@ -295,12 +300,13 @@ __global__ void __launch_bounds__(THREADS, 1)
     const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
     const uint32_t tl = tmem + ((uint32_t)(32 * g) << 16);
     for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t v0[16], v1[16], v2[16], v3[16];
+      uint32_t v0[16], v1[16], v2[16], v3[16], v4[16];
       __syncwarp();
       tmem_ld16(tl + (uint32_t)c0, v0);
       tmem_ld16(tl + (uint32_t)(BN + c0), v1);
       tmem_ld16(tl + (uint32_t)(2 * BN + c0), v2);
       tmem_ld16(tl + (uint32_t)(3 * BN + c0), v3);
+      tmem_ld16(tl + (uint32_t)(4 * BN + c0), v4);
       if (row < p.M) {
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
@@ -309,11 +315,11 @@ __global__ void __launch_bounds__(THREADS, 1)
           double re = 0.0, im = 0.0;
           const int eb = p.eb[col >> 1];
           if (have && ea > EXP_NONE && eb > EXP_NONE) {
-            // value = (sum_s 2^(8 (3 - s)) acc_s) 2^(ea + eb - 38); the level sums are
+            // value = (sum_s 2^(8 (4 - s)) acc_s) 2^(ea + eb - 46); the level sums are
             // integer-valued FP32, combined exactly in int64, one rounding to FP64
-            const int sh = ea + eb - 38;
-            re = combine_levels(v0[j], v1[j], v2[j], v3[j], sh);
-            im = combine_levels(v0[j + 1], v1[j + 1], v2[j + 1], v3[j + 1], sh);
+            const int sh = ea + eb - 46;
+            re = combine_levels(v0[j], v1[j], v2[j], v3[j], v4[j], sh);
+            im = combine_levels(v0[j + 1], v1[j + 1], v2[j + 1], v3[j + 1], v4[j + 1], sh);
           }
           if (p.part != nullptr) {
             double2* dst = reinterpret_cast<double2*>(p.part + ((long)split * p.M + row) * p.N + col);
