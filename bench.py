@@ -59,7 +59,9 @@ def parse():
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
     p.add_argument("--graph", action="store_true")
-    p.add_argument("--workload", default="xxz", choices=["xxz", "ising-batch"])
+    p.add_argument("--workload", default="xxz", choices=["xxz", "ising-batch", "xxz-d1024"])
+    p.add_argument("--dmrg-sweeps", type=int, default=4)
+    p.add_argument("--dmrg-acc-sweeps", type=int, default=1)
     p.add_argument("--batch-count", type=int, default=256)
     p.add_argument("--batch-seed", type=int, default=2027)
     p.add_argument("--streams", type=int, default=None)
@@ -564,6 +566,110 @@ def batch_reference_arm(a):
     print(json.dumps(out))
 
 
+# ------------------------------------------------------------------ precision workload
+PREC_METRIC = "TDVP site-updates/s, XXZ L=32 D=1024, mixed vs FP64 per step; DMRG D=1024"
+
+
+def precision_arm(a):
+    """XXZ L=32 (J=1, Delta=0.8, h=-0.1), bonds min(2^min(i, L-i), 1024), seeded random
+    left-orthonormal MPS; TDVP dt=0.02j, numiter_lanczos=12 in the mixed form (timed over
+    --steps steps) with energy error, norm drift and infidelity against the FP64 form after
+    each of the first --acc-steps steps; then single-site DMRG (--dmrg-sweeps sweeps, mixed)
+    from a seeded random D=1024 state with the FP64 sweeps' energies for the first
+    --dmrg-acc-sweeps sweeps."""
+    import torch
+    import warnings
+    import __graft_entry__
+    __graft_entry__.build()
+    import pytenet_gb300 as ptg
+    from pytenet_gb300 import _lib
+    from pytenet_gb300.chain_ops import mpo_average, mps_vdot
+    _lib.load()
+    L, D, m, dt = 32, 1024, 12, 0.02j
+    rng = np.random.default_rng(a.seed)
+    h = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 0.8, -0.1)
+    h.zero_qnumbers()
+    b = [min(2 ** min(i, L - i), D) for i in range(L + 1)]
+    psi = ptg.MPS(h.qsite, [bi * [0] for bi in b], fill="random", rng=rng)
+    psi.orthonormalize(mode="left")
+    host0 = [x.copy() for x in psi.a]
+
+    def fresh():
+        p = ptg.MPS(psi.qsite, psi.qbonds, fill="postpone")
+        p.a = [x.copy() for x in host0]
+        return p
+
+    # ---- TDVP, mixed, timed; accuracy steps in lockstep with the FP64 form
+    pm, pf = fresh(), fresh()
+    rm = ptg.TDVPRun(h, pm, numiter_lanczos=m, precision="mixed")
+    rf = ptg.TDVPRun(h, pf, numiter_lanczos=m, precision="fp64") if a.acc_steps > 0 else None
+    per_step = []
+    t_acc = 0.0
+    for k in range(a.acc_steps):
+        rm.step(dt)
+        rf.step(dt)
+        rm.download()
+        rf.download()
+        em, ef = mpo_average(pm, h).real, mpo_average(pf, h).real
+        ov = mps_vdot(pf, pm)
+        nm, nf = mps_vdot(pm, pm).real, mps_vdot(pf, pf).real
+        per_step.append({"step": k + 1, "energy_fp64": ef, "energy_mixed": em,
+                         "energy_rel_err": abs(em - ef) / abs(ef),
+                         "infidelity": 1.0 - abs(ov) ** 2 / (nm * nf),
+                         "norm_drift": abs(np.sqrt(nm) - np.sqrt(nf))})
+    del rf
+    warm = max(0, 3 - a.acc_steps)   # at least 3 untimed steps in all
+    for _ in range(warm):
+        rm.step(dt)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", "0")))
+    clocks.start()
+    e0.record()
+    for _ in range(a.steps):
+        rm.step(dt)
+    e1.record()
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    ms = e0.elapsed_time(e1)
+    value = (2 * L - 1) * a.steps / (ms / 1e3)
+    # ---- DMRG from a seeded random D=1024 state
+    rng2 = np.random.default_rng(a.seed + 1)
+    hd = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 0.8, -0.1)
+    hd.zero_qnumbers()
+    p0 = ptg.MPS(hd.qsite, [bi * [0] for bi in b], fill="random", rng=rng2)
+    d0 = [x.copy() for x in p0.a]
+    pdm = ptg.MPS(p0.qsite, p0.qbonds, fill="postpone")
+    pdm.a = [x.copy() for x in d0]
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        t0 = time.perf_counter()
+        en_m = ptg.dmrg_singlesite(hd, pdm, a.dmrg_sweeps, numiter_lanczos=m, precision="mixed")
+        torch.cuda.synchronize()
+        t_dm = time.perf_counter() - t0
+        en_f = []
+        if a.dmrg_acc_sweeps > 0:
+            pdf = ptg.MPS(p0.qsite, p0.qbonds, fill="postpone")
+            pdf.a = [x.copy() for x in d0]
+            en_f = list(ptg.dmrg_singlesite(hd, pdf, a.dmrg_acc_sweeps, numiter_lanczos=m,
+                                            precision="fp64"))
+    dmrg = {"sweeps": a.dmrg_sweeps, "numiter_lanczos": m, "energies_mixed": list(map(float, en_m)),
+            "energies_fp64": list(map(float, en_f)),
+            "energy_rel_err_per_sweep": [abs(float(en_m[k]) - en_f[k]) / abs(en_f[k])
+                                         for k in range(len(en_f))],
+            "site_updates_per_s": 2 * (L - 1) * a.dmrg_sweeps / t_dm, "seconds": t_dm}
+    out = {"metric": PREC_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": 1,
+           "steps": a.steps, "warmup": a.acc_steps + warm, "ms_per_step": ms / a.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "split-bf16 (fp32 acc) + fp64 krylov/qr", "data": "synthetic",
+           "config": {"workload": f"XXZ L={L} D={D} J=1 Delta=0.8 h=-0.1 (seed {a.seed}), "
+                                  f"dt=0.02j, numiter_lanczos={m}; TDVP steps timed after "
+                                  f"{a.acc_steps} accuracy steps",
+                      "l2": "inputs larger than L2"},
+           "clocks": clk, "accuracy_per_step": per_step, "dmrg": dmrg}
+    print(json.dumps(out))
+
+
 def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
     """Energy error, infidelity and norm drift of the benchmarked form (mixed, with
     the learned depth when given) against the plain FP64 fixed-depth form after
@@ -594,6 +700,9 @@ def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
 
 def main():
     a = parse()
+    if a.workload == "xxz-d1024":
+        precision_arm(a)
+        return
     if a.workload == "ising-batch":
         if a.impl == "reference":
             batch_reference_arm(a)
