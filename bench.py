@@ -447,14 +447,17 @@ def batch_arm(a):
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     value = site_updates * a.steps / (ms / 1e3)
+    print(json.dumps({"partial": True, "value": value, "ms_per_step": ms / a.steps,
+                      "tuning": b.tuning, "streams": b.nstreams}), file=sys.stderr, flush=True)
     # kernel split and launch count from one eager step of every instance (graph
-    # replays bypass the host-side hooks)
+    # replays bypass the host-side hooks), under each instance's tuned knobs
     import ctypes
     launches0 = L.ptn_launch_count()
     L.ptn_prof_start(0x1F)
     torch.cuda.synchronize()
-    for r in b.runs:
-        r.chain.tdvp_step(dt)
+    for p, r in zip(psis, b.runs):
+        with b._knobs(p):
+            r.chain.tdvp_step(dt)
     torch.cuda.synchronize()
     L.ptn_prof_stop()
     prof_note = "one eager step of every instance, instance order; the library's hooks keep " \

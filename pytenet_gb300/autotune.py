@@ -3,10 +3,13 @@ Autotuner for the batched driver: per (bond-dimension bucket, d, chi) of the
 batch, the library's launch-shape knobs (ptn_tune_set), and the number of CUDA
 streams the batch is spread over.
 
-Knobs (include/pytenet_gb300.h):
+Knobs (include/pytenet_gb300.h), plus "mmb", the smallest bond on which the mixed form
+uses the tensor cores (a tensor-core GEMM CTA takes a whole SM's shared memory and
+tensor memory, so in a batch small problems may overlap better on the FP64 path):
   PTN_TUNE_TC_SPLIT_WAVES    split-K target of the tensor-core digit GEMM
   PTN_TUNE_ZGEMM_SPLIT_WAVES split-K target of the FP64 GEMM
   PTN_TUNE_LARFB_TILE        block-update tile of the QR
+  PTN_TUNE_QR_CLUSTER        cluster size cap of the QR panel
 Each bucket is tuned on its most expensive instance by coordinate descent: one
 knob at a time over its candidates, the others held, each candidate timed with
 CUDA events over a time step of COPIES concurrent copies of that instance on as
@@ -32,11 +35,13 @@ from .device import lib
 __all__ = ["tune_batch", "knobs_for", "bucket_of", "DEFAULT_KNOBS"]
 
 DEFAULT_KNOBS = {_lib.TUNE_TC_SPLIT_WAVES: 2, _lib.TUNE_ZGEMM_SPLIT_WAVES: 2,
-                 _lib.TUNE_LARFB_TILE: 0}
-CANDIDATES = {_lib.TUNE_TC_SPLIT_WAVES: [1, 2, 4],
-              _lib.TUNE_ZGEMM_SPLIT_WAVES: [0, 1, 2, 4],
-              _lib.TUNE_LARFB_TILE: [0, 1, 3]}
-STREAM_CANDIDATES = [4, 8, 16, 32]
+                 _lib.TUNE_LARFB_TILE: 0, _lib.TUNE_QR_CLUSTER: 0, "mmb": 32}
+CANDIDATES = {"mmb": [32, 64, 128, 1 << 20],
+              _lib.TUNE_TC_SPLIT_WAVES: [0, 2],
+              _lib.TUNE_ZGEMM_SPLIT_WAVES: [0, 2],
+              _lib.TUNE_LARFB_TILE: [0, 1],
+              _lib.TUNE_QR_CLUSTER: [0, 1]}
+STREAM_CANDIDATES = [4, 8, 16]
 COPIES = 4
 _CACHE = {}
 
@@ -53,7 +58,9 @@ def bucket_of(psi, chi=None):
 
 @contextlib.contextmanager
 def knobs(values):
+    """Set the library knobs of `values` (keys that are knob numbers) for the block."""
     L = lib()
+    values = {k: v for k, v in values.items() if str(k).isdigit()}
     old = {int(k): L.ptn_tune_get(int(k)) for k in values}
     try:
         for k, v in values.items():
@@ -64,11 +71,16 @@ def knobs(values):
             L.ptn_tune_set(int(k), int(v))
 
 
+def bucket_values(tuning, psi):
+    """Tuned values of psi's bucket ({} without tuning)."""
+    if not tuning:
+        return {}
+    return tuning["buckets"].get(str(bucket_of(psi)[:2]), {})
+
+
 def knobs_for(tuning, psi):
     """Context setting the tuned knobs of psi's bucket (no-op without tuning)."""
-    if not tuning:
-        return contextlib.nullcontext()
-    vals = tuning["buckets"].get(str(bucket_of(psi)[:2]))
+    vals = bucket_values(tuning, psi)
     return knobs(vals) if vals else contextlib.nullcontext()
 
 
@@ -88,14 +100,15 @@ def _time_step(h, psi, numiter, precision, values, dt):
 
 
 def _tune_bucket(h, psi, numiter, precision, dt):
-    best = dict(DEFAULT_KNOBS)
-    keys = list(CANDIDATES)
+    best = {str(k): v for k, v in DEFAULT_KNOBS.items()}
+    keys = [str(k) for k in CANDIDATES]
     if precision == "fp64":
-        keys.remove(_lib.TUNE_TC_SPLIT_WAVES)
+        keys = [k for k in keys if k not in (str(_lib.TUNE_TC_SPLIT_WAVES), "mmb")]
+    cands = {str(k): v for k, v in CANDIDATES.items()}
     t_best = _time_step(h, psi, numiter, precision, best, dt)
     trials = {json.dumps(best, sort_keys=True): t_best}
     for k in keys:
-        for v in CANDIDATES[k]:
+        for v in cands[k]:
             cand = dict(best)
             cand[k] = v
             key = json.dumps(cand, sort_keys=True)
@@ -106,7 +119,7 @@ def _tune_bucket(h, psi, numiter, precision, dt):
     return best, t_best
 
 
-def tune_batch(hamiltonians, psis, numiter_lanczos, precision, dt=0.05, subset=32):
+def tune_batch(hamiltonians, psis, numiter_lanczos, precision, dt=0.05, subset=16):
     """Knobs per bucket and the stream count for this batch (cached)."""
     from .batch import BatchTDVP, instance_cost
     sig = (tuple(sorted({bucket_of(p)[:2] for p in psis})), numiter_lanczos, precision)

@@ -81,7 +81,8 @@ class BatchTDVP:
                 for i in grp:
                     with self._knobs(psis[i]):
                         self.runs[i] = TDVPRun(hamiltonians[i], psis[i], numiter_lanczos,
-                                               precision, graph=graph)
+                                               precision, graph=graph,
+                                               mixed_min_bond=self._mixed_min_bond(psis[i]))
         for s in self.streams:
             main.wait_stream(s)
         self.steps_done = 0
@@ -89,6 +90,11 @@ class BatchTDVP:
     def _knobs(self, psi):
         from .autotune import knobs_for
         return knobs_for(self.tuning, psi)
+
+    def _mixed_min_bond(self, psi):
+        from .autotune import bucket_values
+        v = bucket_values(self.tuning, psi).get("mmb")
+        return None if v is None else int(v)
 
     def step(self, dt, capture=True):
         """Exactly one time step of every instance (capture: record each

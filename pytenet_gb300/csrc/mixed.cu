@@ -168,6 +168,22 @@ struct Carver {
   }
 };
 
+// The split-K scratch of the digit GEMMs is the last piece of every workspace
+// layout: give the GEMMs all that the caller's workspace has left (the GEMM picks
+// its K splits to fit, never below what exact accumulation needs), so a workspace
+// sized under other tuning-knob values still works.
+template <class W>
+void use_rest(W& w, void* ws, size_t ws_bytes) {
+  const size_t off = (size_t)(static_cast<char*>(w.gws) - static_cast<char*>(ws));
+  w.gbytes = ws_bytes > off ? ws_bytes - off : 0;
+}
+
+// bytes a layout needs before its GEMM scratch
+template <class W>
+size_t before_gemm(const Carver& c, const W& w) {
+  return c.off - al(w.gbytes);
+}
+
 // BF16 digit planes of a complex matrix with `rows` rows (2 * rows real rows when
 // embedded) and kc complex columns, plus the per-row exponents
 struct Digits {
@@ -303,8 +319,11 @@ ptn_status heff_prepare_mixed(const double2* w, const double2* l, const double2*
                               int Dr, int chil, int chir, void* ws, size_t ws_bytes,
                               cudaStream_t st) {
   (void)w;
-  PTN_CHECK_ARG(ws_bytes >= heff_workspace_bytes_mixed(Dl, d, Dr, chil, chir),
-                "mixed heff: workspace too small");
+  {
+    Carver q(nullptr);
+    const HeffWs hq = heff_ws(q, Dl, d, Dr, chil, chir);
+    PTN_CHECK_ARG(ws_bytes >= before_gemm(q, hq), "mixed heff: workspace too small");
+  }
   Carver c(ws);
   HeffWs h = heff_ws(c, Dl, d, Dr, chil, chir);
   // Rt: (m = (wr, r2), k = r0) = R[r0][(wr, r2)]
@@ -317,9 +336,9 @@ ptn_status heff_prepare_mixed(const double2* w, const double2* l, const double2*
 ptn_status heff_apply_mixed(const double2* x, double2* y, const double2* w, int Dl, int d, int Dr,
                             int chil, int chir, void* ws, size_t ws_bytes, const int* skip,
                             cudaStream_t st) {
-  (void)ws_bytes;
   Carver c(ws);
   HeffWs h = heff_ws(c, Dl, d, Dr, chil, chir);
+  use_rest(h, ws, ws_bytes);
   // Xe: (n = (l0, t), k = r0) = x[(l0, t)][r0]
   PTN_TRY(to_digits(x, Dr, 1, h.Xe, false, skip, st));
   // T1[(l0,t)][(wr,r2)] via T1^T = Rt . Xe^T
@@ -349,7 +368,11 @@ size_t bond_workspace_bytes_mixed(int Dl, int Dr, int chi) {
 
 ptn_status bond_prepare_mixed(const double2* l, const double2* r, int Dl, int Dr, int chi, void* ws,
                               size_t ws_bytes, cudaStream_t st) {
-  PTN_CHECK_ARG(ws_bytes >= bond_workspace_bytes_mixed(Dl, Dr, chi), "mixed bond: workspace too small");
+  {
+    Carver q(nullptr);
+    const BondWs bq = bond_ws(q, Dl, Dr, chi);
+    PTN_CHECK_ARG(ws_bytes >= before_gemm(q, bq), "mixed bond: workspace too small");
+  }
   Carver c(ws);
   BondWs b = bond_ws(c, Dl, Dr, chi);
   PTN_TRY(to_digits(r, 1, (long)chi * Dr, b.Rt, false, nullptr, st));
@@ -359,9 +382,9 @@ ptn_status bond_prepare_mixed(const double2* l, const double2* r, int Dl, int Dr
 
 ptn_status bond_apply_mixed(const double2* x, double2* y, int Dl, int Dr, int chi, void* ws,
                             size_t ws_bytes, const int* skip, cudaStream_t st) {
-  (void)ws_bytes;
   Carver c(ws);
   BondWs b = bond_ws(c, Dl, Dr, chi);
+  use_rest(b, ws, ws_bytes);
   // Xe: (n = l0, k = r0) = C[l0][r0]
   PTN_TRY(to_digits(x, Dr, 1, b.Xe, false, skip, st));
   // T1[l0][(w, r2)] via T1^T = Rt . Xe^T
@@ -392,9 +415,10 @@ size_t env_workspace_bytes_mixed(int Dl, int d, int Dr, int cl, int cr) {
 ptn_status env_left_mixed(const double2* a, const double2* b, const double2* w, const double2* l,
                           double2* lnext, int Dl, int d, int Dr, int cl, int cr, void* ws,
                           size_t ws_bytes, cudaStream_t st) {
-  PTN_CHECK_ARG(ws_bytes >= env_workspace_bytes_mixed(Dl, d, Dr, cl, cr), "mixed env: workspace too small");
   Carver c(ws);
   EnvWs e = env_left_ws(c, Dl, d, Dr, cl, cr);
+  PTN_CHECK_ARG(ws_bytes >= before_gemm(c, e), "mixed env: workspace too small");
+  use_rest(e, ws, ws_bytes);
   // S1: (m = (t, rb), k = l2) = conj(B[l2][(t, rb)])
   PTN_TRY(to_digits(b, 1, (long)d * Dr, e.S1, true, nullptr, st));
   // E1: (n = (l0, wl), k = l2) = L[(l0, wl)][l2]
@@ -416,9 +440,10 @@ ptn_status env_left_mixed(const double2* a, const double2* b, const double2* w, 
 ptn_status env_right_mixed(const double2* a, const double2* b, const double2* w, const double2* r,
                            double2* rnext, int Dl, int d, int Dr, int cl, int cr, void* ws,
                            size_t ws_bytes, cudaStream_t st) {
-  PTN_CHECK_ARG(ws_bytes >= env_workspace_bytes_mixed(Dl, d, Dr, cl, cr), "mixed env: workspace too small");
   Carver c(ws);
   EnvWs e = env_right_ws(c, Dl, d, Dr, cl, cr);
+  PTN_CHECK_ARG(ws_bytes >= before_gemm(c, e), "mixed env: workspace too small");
+  use_rest(e, ws, ws_bytes);
   // S1: (m = (wr, r2), k = r0) = R[r0][(wr, r2)]
   PTN_TRY(to_digits(r, 1, (long)cr * Dr, e.S1, false, nullptr, st));
   // E1: (n = (l0, s), k = r0) = A[(l0, s)][r0]
@@ -449,12 +474,12 @@ size_t zgemm_split_workspace_bytes(int M, int N, int K) {
 ptn_status zgemm_split(const double2* A, long lda, const double2* B, long ldb, double2* C, long ldc,
                        int M, int N, int K, void* ws, size_t ws_bytes, cudaStream_t st) {
   PTN_CHECK_ARG(M > 0 && N > 0 && K > 0, "zgemm_split: bad sizes");
-  PTN_CHECK_ARG(ws_bytes >= zgemm_split_workspace_bytes(M, N, K), "zgemm_split: workspace too small");
   Carver c(ws);
   Digits As = take_digits(c, M, K, false);
   Digits Bs = take_digits(c, N, K, true);
-  const size_t gb = tc_gemm_workspace_bytes(M, N, K);
-  void* g = c.take(gb);
+  PTN_CHECK_ARG(ws_bytes >= c.off, "zgemm_split: workspace too small");
+  void* g = c.take(0);
+  const size_t gb = ws_bytes - c.off;
   PTN_TRY(to_digits(A, lda, 1, As, false, nullptr, st));
   // B as the view (n, k) = B[k][n]
   PTN_TRY(to_digits(B, 1, ldb, Bs, false, nullptr, st));

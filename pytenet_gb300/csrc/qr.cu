@@ -1042,9 +1042,16 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
   // LAPACK flop count of zgeqrf + zungqr (4 real flops per complex op)
   const double fq = 8.0 * ((double)m * n * k - (double)(m + n) * k * k / 2.0 + (double)k * k * k / 3.0);
   const int prof = prof_begin(st, PROF_QR, 2.0 * fq, 16.0 * 3.0 * m * n);
-  const int cs = panel_cluster_size();
+  const int cs_max = panel_cluster_size();
+  const int cap = tune(PTN_TUNE_QR_CLUSTER);
   for (int j0 = 0, p = 0; j0 < k; j0 += NB, ++p) {
     const int jb = std::min(NB, k - j0);
+    // cluster of the panel: at least 32 rows per CTA (power of two), at most the
+    // device's largest cluster and the tuning cap; small panels take few CTAs and so
+    // leave the other SMs of the GPC to concurrent work
+    int cs = 1;
+    while (cs < cs_max && cs * 32 < m - j0) cs *= 2;
+    if (cap > 0) cs = std::min(cs, cap);
     const int chunk = cs > 1 ? (m - j0 + cs - 1) / cs : m - j0;
     if (cs > 1 && chunk <= QW * 32) {
       cudaLaunchConfig_t cfg = {};

@@ -219,10 +219,11 @@ class DepthState:
 class Chain(DeviceMPS):
     """Device state of one TDVP / DMRG run: MPS, MPO, environments, Krylov buffers."""
 
-    def __init__(self, op, psi, numiter, precision="fp64", depth=None):
+    def __init__(self, op, psi, numiter, precision="fp64", depth=None, mixed_min_bond=None):
         assert len(op.a) == len(psi.a)
         super().__init__(psi)
         self.prec = prec_code(precision)
+        self.mixed_min_bond = MIXED_MIN_BOND if mixed_min_bond is None else int(mixed_min_bond)
         self.numiter = int(numiter)
         if not 1 <= self.numiter < _lib.KRYLOV_MAXITER:
             raise ValueError(f"numiter_lanczos must be in [1, {_lib.KRYLOV_MAXITER})")
@@ -256,11 +257,14 @@ class Chain(DeviceMPS):
 
     def prec_for(self, Dl, Dr):
         """Arithmetic of one local problem. The mixed form runs the tensor-core digit
-        GEMMs only where both bonds reach MIXED_MIN_BOND: below that the contractions
-        are too small to fill a 128 x 128 tile, and the Krylov space of a small
-        problem can be exhausted (a Lanczos breakdown at beta < 100 n eps), which
-        only the FP64 operator detects the way the reference does."""
-        if self.prec != _lib.PREC_FP64 and min(Dl, Dr) < MIXED_MIN_BOND:
+        GEMMs only where both bonds reach mixed_min_bond (MIXED_MIN_BOND unless set):
+        below that the contractions are too small to fill a 128 x 96 tile, and the
+        Krylov space of a small problem can be exhausted (a Lanczos breakdown at
+        beta < 100 n eps), which only the FP64 operator detects the way the reference
+        does. The batched driver raises it per bucket: a tensor-core GEMM CTA takes a
+        whole SM's shared memory and tensor memory, so small problems of concurrent
+        instances overlap better on the FP64 path."""
+        if self.prec != _lib.PREC_FP64 and min(Dl, Dr) < self.mixed_min_bond:
             return _lib.PREC_FP64
         return self.prec
 

@@ -20,10 +20,12 @@ class TDVPRun:
     depth the run falls back to whenever the residual estimate at the predicted
     depth exceeds depth_tol.
     graph: capture one time step in a CUDA graph after the first step and
-    replay it (all buffers are preallocated and no step synchronises)."""
+    replay it (all buffers are preallocated and no step synchronises).
+    mixed_min_bond: smallest bond on which the mixed form uses the tensor cores
+    (default engine.MIXED_MIN_BOND)."""
 
     def __init__(self, hamiltonian, psi, numiter_lanczos=25, precision="fp64", graph=False,
-                 depth_model=None, depth_tol=1e-10, record_capacity=0):
+                 depth_model=None, depth_tol=1e-10, record_capacity=0, mixed_min_bond=None):
         nsites = len(hamiltonian.a)
         assert nsites == len(psi.a)
         self.psi = psi
@@ -32,7 +34,8 @@ class TDVPRun:
             from .engine import DepthState
             params = depth_model.params if depth_model is not None else None
             depth = DepthState(nsites, params, depth_tol, record_capacity)
-        self.chain = Chain(hamiltonian, psi, numiter_lanczos, precision, depth=depth)
+        self.chain = Chain(hamiltonian, psi, numiter_lanczos, precision, depth=depth,
+                           mixed_min_bond=mixed_min_bond)
         # right-normalise, build the environments (pytenet/tdvp.py:51-63)
         self.nrm = self.chain.orthonormalize("right").clone()
         self.chain.init_envs()
