@@ -227,6 +227,22 @@ class ClockSampler:
 
 
 # ------------------------------------------------------------------ our arm
+def max_over_ranks(ms, device):
+    """Slowest rank's time (replicas run the same workload; the job takes as long
+    as its slowest replica)."""
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    if dist.is_available() and dist.is_initialized() and dist.get_world_size() > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(world, site_updates, steps, ms_max):
+    """Whole-job site-updates/s of `world` independent replicas (weak scaling)."""
+    return world * site_updates * steps / (ms_max / 1e3)
+
+
 def our_arm(a):
     import torch
     import torch.distributed as dist
@@ -287,11 +303,8 @@ def our_arm(a):
               "depth_tol": a.depth_tol if a.form == "learned" else None}
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = world * site_updates * a.steps / (ms_max / 1e3)
+    ms_max = max_over_ranks(ms, "cuda")
+    value = replica_value(world, site_updates, a.steps, ms_max)
 
     def prof(kind):
         import ctypes
@@ -586,7 +599,6 @@ def precision_arm(a):
     __graft_entry__.build()
     import pytenet_gb300 as ptg
     from pytenet_gb300 import _lib
-    from pytenet_gb300.chain_ops import mpo_average, mps_vdot
     _lib.load()
     L, D, m, dt = 32, 1024, 12, 0.02j
     rng = np.random.default_rng(a.seed)
@@ -611,11 +623,10 @@ def precision_arm(a):
     for k in range(a.acc_steps):
         rm.step(dt)
         rf.step(dt)
-        rm.download()
-        rf.download()
-        em, ef = mpo_average(pm, h).real, mpo_average(pf, h).real
-        ov = mps_vdot(pf, pm)
-        nm, nf = mps_vdot(pm, pm).real, mps_vdot(pf, pf).real
+        # contracted on the device from the runs' resident tensors (no download)
+        em, ef = rm.energy().real, rf.energy().real
+        ov = rm.vdot(rf)
+        nm, nf = rm.vdot(rm).real, rf.vdot(rf).real
         per_step.append({"step": k + 1, "energy_fp64": ef, "energy_mixed": em,
                          "energy_rel_err": abs(em - ef) / abs(ef),
                          "infidelity": 1.0 - abs(ov) ** 2 / (nm * nf),

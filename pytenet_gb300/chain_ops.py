@@ -113,16 +113,24 @@ def compute_right_operator_blocks(psi, op):
     return blocks
 
 
+def _tensors(x):
+    """Site tensors of an MPS / MPO (host arrays, uploaded per use) or a list of
+    device tensors (a device-resident run's sites: no host round trip)."""
+    return x.a if hasattr(x, "a") else list(x)
+
+
 def mpo_inner_product(chi, op, psi):
     """<chi|op|psi> (pytenet/chain_ops.py:165-189); chi and psi must share their
-    bond dimensions (the square-environment kernels)."""
-    assert chi.nsites == op.nsites and psi.nsites == op.nsites
-    if psi.nsites == 0:
+    bond dimensions (the square-environment kernels). Each argument is an MPS /
+    MPO or a list of device site tensors."""
+    A, B, W = _tensors(psi), _tensors(chi), _tensors(op)
+    assert len(A) == len(B) == len(W)
+    if len(A) == 0:
         return 0
-    n = psi.a[-1].shape[2]
+    n = A[-1].shape[2]
     t = to_dev(np.identity(n).reshape((n, 1, n)))
-    for i in reversed(range(psi.nsites)):
-        t = contraction_operator_step_right(to_dev(psi.a[i]), to_dev(chi.a[i]), to_dev(op.a[i]), t)
+    for i in reversed(range(len(A))):
+        t = contraction_operator_step_right(to_dev(A[i]), to_dev(B[i]), to_dev(W[i]), t)
     assert tuple(t.shape) == (1, 1, 1)
     return complex(t.reshape(-1)[0].item())
 
@@ -140,15 +148,17 @@ def _zgemm(opa, opb, M, N, K, A, lda, B, ldb, Cout, ldc):
 
 
 def mps_vdot(chi, psi):
-    """<chi|psi> (pytenet/mps.py:430-450), contracted from the right on the GPU."""
-    assert chi.nsites == psi.nsites
-    if psi.nsites == 0:
+    """<chi|psi> (pytenet/mps.py:430-450), contracted from the right on the GPU;
+    chi and psi are MPS or lists of device site tensors."""
+    A, B = _tensors(psi), _tensors(chi)
+    assert len(A) == len(B)
+    if len(A) == 0:
         return 0
-    n = psi.a[-1].shape[2]
+    n = A[-1].shape[2]
     t = to_dev(np.identity(n))               # (Dpsi_r, Dchi_r)
-    for i in reversed(range(psi.nsites)):
-        a = to_dev(psi.a[i])
-        b = to_dev(chi.a[i])
+    for i in reversed(range(len(A))):
+        a = to_dev(A[i])
+        b = to_dev(B[i])
         Dl, d, Dr = a.shape
         El, _, Er = b.shape
         # u[(l, s), e] = sum_r a[(l, s), r] t[r, e]

@@ -739,12 +739,13 @@ __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict_
       tot = vals[0];
     }
     if (rank == 0 && warp == 0 && lane < jj) s_G[lane][jj] = tot;
-    // ---- rank-1 update of this thread's row
-    const double2 ctau = cconj(tau);
+    // ---- rank-1 update of this thread's row: x_c -= v conj(tau) w_c, with the
+    // scalar conj(tau) w_c formed once per column (lane c) and broadcast
+    const double2 sc = (lane < NB) ? cmul(cconj(tau), tot) : c2(0.0, 0.0);
 #pragma unroll
     for (int c = 0; c < NB; ++c) {
-      const double2 wcc = c2(__shfl_sync(0xffffffffu, tot.x, c), __shfl_sync(0xffffffffu, tot.y, c));
-      if (c > jj && apply && mine && i >= col) xs[c][tid] = csub(xs[c][tid], cmul(vcur, cmul(ctau, wcc)));
+      const double2 s = c2(__shfl_sync(0xffffffffu, sc.x, c), __shfl_sync(0xffffffffu, sc.y, c));
+      if (c > jj && apply && mine && i >= col) xs[c][tid] = csub(xs[c][tid], cmul(vcur, s));
     }
   }
 

@@ -417,7 +417,7 @@ MapCache& map_cache() {
 }
 
 // 3-D map over digit planes [4][rows][Kp] of BF16, logical extent (K, rows, 4),
-// box (BK, box_rows, 4): one load brings a K block of all four planes
+// box (BK, box_rows, 5): one load brings a K block of all five planes
 bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, long plane,
               int box_rows) {
   MapKey key{ptr, rows, K, Kp, plane, box_rows};

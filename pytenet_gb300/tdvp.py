@@ -78,6 +78,26 @@ class TDVPRun:
         self.chain.download(self.psi)
         return self.psi
 
+    # ------------------------------------------------ measurements on the device
+    def tensors(self):
+        """Current site tensors as device views (no copy)."""
+        return [self.chain.site(i) for i in range(self.chain.nsites)]
+
+    def energy(self):
+        """<psi|H|psi> of the current state, contracted in FP64 on the device
+        (pytenet/chain_ops.py:151-162 without the host round trip)."""
+        from .chain_ops import mpo_average
+        return mpo_average(self.tensors(), self.chain.w)
+
+    def vdot(self, other):
+        """<other|psi> against another run (or MPS / tensor list) of equal bonds."""
+        from .chain_ops import mps_vdot
+        o = other.tensors() if isinstance(other, TDVPRun) else other
+        return mps_vdot(o, self.tensors())
+
+    def norm(self):
+        return float(np.sqrt(self.vdot(self).real))
+
 
 def tdvp_singlesite(hamiltonian, psi, dt, numsteps, numiter_lanczos=25, precision="fp64",
                     graph=False, depth_model=None, depth_tol=1e-10):

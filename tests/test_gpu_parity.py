@@ -291,3 +291,21 @@ def test_dmrg_singlesite_golden(ptg):
         assert np.array_equal(qa, qb)
     v = psi.to_vector()
     assert abs(abs(np.vdot(v, g["v1"])) - 1) < 1e-9
+
+
+def test_run_measurements_on_device(ptg):
+    """TDVPRun.energy / vdot contract the resident tensors on the device and agree
+    with the oracle on the downloaded state (pytenet/chain_ops.py:151-189)."""
+    rng = np.random.default_rng(8)
+    L = 10
+    h = ptg.heisenberg_xxz_1d_mpo(L, 1.0, 0.8, -0.1)
+    h.zero_qnumbers()
+    b = [min(2 ** min(i, L - i), 8) for i in range(L + 1)]
+    psi = ptg.MPS(h.qsite, [bi * [0] for bi in b], fill="random", rng=rng)
+    psi.orthonormalize(mode="left")
+    run = ptg.TDVPRun(h, psi, numiter_lanczos=6)
+    run.step(0.1j)
+    e_dev, n_dev = run.energy(), run.norm()
+    run.download()
+    assert abs(e_dev - orc.mpo_average(psi, h)) < 1e-12 * max(1.0, abs(e_dev))
+    assert abs(n_dev ** 2 - orc.mps_vdot(psi, psi).real) < 1e-12
