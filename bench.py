@@ -49,6 +49,8 @@ def parse():
     p.add_argument("--form", default=os.environ.get("PTN_BENCH_FORM", "learned"),
                    choices=["learned", "mixed", "fp64"])
     p.add_argument("--depth-tol", type=float, default=1e-10)
+    p.add_argument("--tc-split-waves", type=int, default=None,
+                   help="PTN_TUNE_TC_SPLIT_WAVES for the run (library default if unset)")
     p.add_argument("--L", type=int, default=64)
     p.add_argument("--D", type=int, default=512)
     p.add_argument("--m", type=int, default=10)
@@ -258,6 +260,8 @@ def our_arm(a):
     from pytenet_gb300 import _lib
     L = _lib.load()
 
+    if a.tc_split_waves is not None:
+        _lib.check(L.ptn_tune_set(_lib.TUNE_TC_SPLIT_WAVES, a.tc_split_waves))
     h, psi, delta = make_workload(a, ptg)
     psi.orthonormalize(mode="left")
     psi_host0 = [x.copy() for x in psi.a]
@@ -381,6 +385,7 @@ def our_arm(a):
                "data": "synthetic",
                "config": {"workload": workload_desc(a), "form": a.form, "L": a.L, "D": a.D,
                           "numiter_lanczos": a.m, "delta": delta, "graph": a.graph,
+                          "tc_split_waves": L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES),
                           "parallelism": f"replicas x{world}",
                           "l2": "inputs larger than L2 (state of several GB per replica)"},
                "krylov": krylov, "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,

@@ -87,7 +87,7 @@ uint64_t ptn_launch_count(void);
  * launch shape on the host, so a CUDA graph keeps the values it was captured
  * with; workspace queries read them too (query and call under the same values).
  *   PTN_TUNE_TC_SPLIT_WAVES    split-K of the tensor-core GEMM aims at this many
- *                              waves of CTAs (0..16, default 2; never fewer
+ *                              waves of CTAs (0..16, default 1; never fewer
  *                              splits than exact integer accumulation needs)
  *   PTN_TUNE_ZGEMM_SPLIT_WAVES split-K target of the FP64 GEMM (0..16, default 2;
  *                              0 = no split-K)

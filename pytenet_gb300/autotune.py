@@ -34,7 +34,7 @@ from .device import lib
 
 __all__ = ["tune_batch", "knobs_for", "bucket_of", "DEFAULT_KNOBS"]
 
-DEFAULT_KNOBS = {_lib.TUNE_TC_SPLIT_WAVES: 2, _lib.TUNE_ZGEMM_SPLIT_WAVES: 2,
+DEFAULT_KNOBS = {_lib.TUNE_TC_SPLIT_WAVES: 1, _lib.TUNE_ZGEMM_SPLIT_WAVES: 2,
                  _lib.TUNE_LARFB_TILE: 0, _lib.TUNE_QR_CLUSTER: 0, "mmb": 32}
 CANDIDATES = {"mmb": [32, 64, 128, 1 << 20],
               _lib.TUNE_TC_SPLIT_WAVES: [0, 2],

@@ -1054,7 +1054,7 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
     while (cs < cs_max && cs * 32 < m - j0) cs *= 2;
     if (cap > 0) cs = std::min(cs, cap);
     const int chunk = cs > 1 ? (m - j0 + cs - 1) / cs : m - j0;
-    if (cs > 1 && chunk <= QW * 32) {
+    if (chunk <= QW * 32) {   // a cluster of one CTA is the single-CTA case
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs);
       cfg.blockDim = dim3(32 * ((chunk + 31) / 32));   // warps the row chunk needs

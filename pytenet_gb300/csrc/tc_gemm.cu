@@ -63,7 +63,7 @@ constexpr int MAX_K_SPLIT = 2048;
 constexpr int THREADS = 192;
 constexpr int TMEM_USED = NLEVEL * BN;   // 480: one accumulator per level
 constexpr int TMEM_COLS = 512;           // allocation (a power of two)
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;   // + barriers, column exponents
 constexpr long WAIT_LIMIT = 1L << 22;
 // kind::f16 instruction descriptor: FP32 accumulate (bit 4), A and B BF16
 // (bits 7, 10), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
@@ -159,6 +159,7 @@ __device__ __forceinline__ void umma_commit(uint64_t* bar) {
                : "memory");
 }
 
+// issue one 32-lane x 16-column load from tensor memory (complete at tmem_wait_ld)
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
   asm volatile(
       "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15},"
@@ -167,7 +168,17 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
         "=r"(v[7]), "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]),
         "=r"(v[14]), "=r"(v[15])
       : "r"(taddr));
+}
+
+__device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+// keeps every use of v after the preceding tcgen05.wait::ld: the empty volatile
+// statements stay in order behind it and redefine the registers
+__device__ __forceinline__ void after_wait(uint32_t (&v)[16]) {
+#pragma unroll
+  for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(v[i]));
 }
 
 // sum_s 2^(8 (4 - s)) acc_s of five integer-valued FP32 level sums, times 2^sh.
@@ -205,6 +216,7 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint64_t* tfull = empty + STAGES;
   uint32_t* tslot = reinterpret_cast<uint32_t*>(tfull + 1);
   int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+  int* s_eb = abort_flag + 1;   // column exponents of this tile (BN / 2 complex columns)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.y * BM, n0 = blockIdx.x * BN;
@@ -290,14 +302,22 @@ __global__ void __launch_bounds__(THREADS, 1)
     if (issued > 0) umma_commit(tfull);
     else mbar_arrive(tfull);
   } else if (warp >= 2) {
-    // ---------------- epilogue: 4 level accumulators -> FP64 -> global
+    // ---------------- epilogue: 5 level accumulators -> FP64 -> global
+    // exponents first, while the main loop runs: the row's in a register, the
+    // tile's column exponents in shared memory (epilogue warps' named barrier)
+    const int g = warp & 3;
+    const int row = m0 + 32 * g + lane;
+    const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
+    if (warp == 2)
+      for (int c = lane; c < BN / 2; c += 32) {
+        const int col = (n0 >> 1) + c;
+        s_eb[c] = (2 * col < p.N) ? p.eb[col] : EXP_NONE - 1;
+      }
+    asm volatile("bar.sync 1, 128;" ::: "memory");
     const bool ok = mbar_wait(tfull, 0);
     if (!ok) atomicExch(p.err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const int g = warp & 3;
-    const int row = m0 + 32 * g + lane;
     const bool have = ok && (it1 > it0) && !*(volatile int*)abort_flag;
-    const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
     const uint32_t tl = tmem + ((uint32_t)(32 * g) << 16);
     for (int c0 = 0; c0 < BN; c0 += 16) {
       uint32_t v0[16], v1[16], v2[16], v3[16], v4[16];
@@ -307,13 +327,19 @@ __global__ void __launch_bounds__(THREADS, 1)
       tmem_ld16(tl + (uint32_t)(2 * BN + c0), v2);
       tmem_ld16(tl + (uint32_t)(3 * BN + c0), v3);
       tmem_ld16(tl + (uint32_t)(4 * BN + c0), v4);
+      tmem_wait_ld();
+      after_wait(v0);
+      after_wait(v1);
+      after_wait(v2);
+      after_wait(v3);
+      after_wait(v4);
       if (row < p.M) {
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
           const int col = n0 + c0 + j;
           if (col >= p.N) break;
           double re = 0.0, im = 0.0;
-          const int eb = p.eb[col >> 1];
+          const int eb = s_eb[(c0 + j) >> 1];
           if (have && ea > EXP_NONE && eb > EXP_NONE) {
             // value = (sum_s 2^(8 (4 - s)) acc_s) 2^(ea + eb - 46); the level sums are
             // integer-valued FP32, combined exactly in int64, one rounding to FP64

@@ -47,4 +47,4 @@ def test_tuning_knobs_validate_and_round_trip():
         assert L.ptn_tune_set(k, old) == _lib.PTN_OK
     assert L.ptn_tune_set(_lib.TUNE_LARFB_TILE, 9) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_set(7, 1) == _lib.PTN_BAD_SHAPE
-    assert L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES) == 2
+    assert L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES) == 1
