@@ -359,8 +359,12 @@ def our_arm(a):
         achieved = k_fl / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
         unit = "TFLOP/s"
         kern = "DMMA complex128 GEMM"
+    # DRAM bytes per launch of the dominant kernel from one ncu capture of the same GEMM
+    # shapes (profiles/tc_gemm_xxz_L24_D512.md: mean of the two captured launches)
+    traffic = 50.0e6 if dominant == 1 and a.D == 512 else None
     roofline = {"bound": "tensor", "kernel": kern, "achieved": achieved, "peak": peak,
-                "unit": unit, "frac": (achieved / peak) if achieved else None, "traffic": None,
+                "unit": unit, "frac": (achieved / peak) if achieved else None, "traffic": traffic,
+                "traffic_unit": "bytes per launch (ncu capture at D=512)" if traffic else None,
                 "peak_source": peak_src, "launches_timed": k_n,
                 "kernel_share_of_step": (k_ms / prof_ms) if prof_ms > 0 else None,
                 "qr_share_of_step": (q_ms / prof_ms) if prof_ms > 0 else None,
