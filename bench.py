@@ -360,7 +360,7 @@ def our_arm(a):
         unit = "TFLOP/s"
         kern = "DMMA complex128 GEMM"
     # DRAM bytes per launch of the dominant kernel from one ncu capture of the same GEMM
-    # shapes (profiles/tc_gemm_xxz_L24_D512.md: mean of the two captured launches)
+    # shapes (the L=24, D=512 workload, bulk-site launches 481-482: mean of the two)
     traffic = 50.0e6 if dominant == 1 and a.D == 512 else None
     roofline = {"bound": "tensor", "kernel": kern, "achieved": achieved, "peak": peak,
                 "unit": unit, "frac": (achieved / peak) if achieved else None, "traffic": traffic,
