@@ -489,15 +489,32 @@ int* err_flag() {
 
 }  // namespace
 
+// K splits: at least what exact integer accumulation needs (MAX_K_SPLIT reals per
+// split), at most enough CTAs for twice PTN_TUNE_TC_SPLIT_WAVES waves (one CTA per SM);
+// in between, the split count with the fewest waves x (K blocks per CTA + a fixed
+// per-CTA cost of prologue and epilogue, about KB_OVERHEAD K blocks) -- a grid that
+// spills a few CTAs into another wave costs that whole wave.
 static int choose_splits(int M, int N, int nkb) {
-  const int tiles = ((N + BN - 1) / BN) * ((M + BM - 1) / BM);
-  const int target = tune(PTN_TUNE_TC_SPLIT_WAVES) * num_sms();
-  int splits = 1;
-  if (tiles < target) splits = std::max(1, std::min((target + tiles - 1) / tiles, nkb / 2));
-  // keep each split's exact integer sums short: at most MAX_K_SPLIT reals per split
-  constexpr int kb_max = MAX_K_SPLIT / BK;
-  splits = std::max(splits, (nkb + kb_max - 1) / kb_max);
-  return std::min(splits, nkb);
+  constexpr int KB_OVERHEAD = 6;
+  const long tiles = (long)((N + BN - 1) / BN) * ((M + BM - 1) / BM);
+  const long sms = num_sms();
+  const int kb_max = MAX_K_SPLIT / BK;
+  const int s_min = std::max(1, (nkb + kb_max - 1) / kb_max);
+  const int waves = tune(PTN_TUNE_TC_SPLIT_WAVES);
+  if (waves == 0) return std::min(s_min, std::max(1, nkb));
+  const long s_cap =
+      std::max<long>(s_min, std::min<long>(nkb, (2L * waves * sms + tiles - 1) / tiles));
+  int best = s_min;
+  long best_cost = -1;
+  for (long s = s_min; s <= s_cap; ++s) {
+    const long w = (tiles * s + sms - 1) / sms;
+    const long cost = w * ((nkb + s - 1) / s + KB_OVERHEAD);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = (int)s;
+    }
+  }
+  return std::min(best, std::max(1, nkb));
 }
 
 size_t tc_gemm_workspace_bytes(int M, int Ncomplex, int Kcomplex) {

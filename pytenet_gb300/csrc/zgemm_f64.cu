@@ -244,15 +244,30 @@ void launch_b(int ob, dim3 grid, cudaStream_t st, const KArgs& k) {
   }
 }
 
+// K splits for skinny problems: up to PTN_TUNE_ZGEMM_SPLIT_WAVES waves of CTAs (at
+// most 32 splits of at least 4 K slabs), choosing the count with the fewest
+// waves x (K slabs per CTA + a fixed per-CTA cost of about SLAB_OVERHEAD slabs).
 int choose_splits(int M, int N, int K, int batch) {
+  constexpr int SLAB_OVERHEAD = 4;
   const long tiles = (long)((M + BM - 1) / BM) * ((N + BN - 1) / BN) * batch;
-  const int sms = num_sms();
+  const long sms = num_sms();
   const int waves = tune(PTN_TUNE_ZGEMM_SPLIT_WAVES);
   if (waves == 0 || tiles >= (long)waves * sms || K < 8 * BK) return 1;
-  int s = (int)(((long)waves * sms + tiles - 1) / tiles);
-  s = std::min(s, K / (4 * BK));
-  s = std::min(s, 32);
-  return std::max(s, 1);
+  const long slabs = (K + BK - 1) / BK;
+  long s_cap = ((long)waves * sms + tiles - 1) / tiles;
+  s_cap = std::min<long>(s_cap, std::max(1, K / (4 * BK)));
+  s_cap = std::min<long>(s_cap, 32);
+  int best = 1;
+  long best_cost = -1;
+  for (long s = 1; s <= s_cap; ++s) {
+    const long w = (tiles * s + sms - 1) / sms;
+    const long cost = w * ((slabs + s - 1) / s + SLAB_OVERHEAD);
+    if (best_cost < 0 || cost < best_cost) {
+      best_cost = cost;
+      best = (int)s;
+    }
+  }
+  return best;
 }
 
 }  // namespace
