@@ -354,250 +354,14 @@ __global__ void __launch_bounds__(CPT) qr_panel_cluster_kernel(double2* __restri
   cluster.sync();   // no CTA leaves while its shared memory may still be read
 }
 
-// Latency-lean panel factorisation: a cluster of CS CTAs of ONE warp each. CTA
-// `rank` owns rows [j0 + rank*chunk, ...) and keeps them in registers (lane l,
-// slot t holds local row t*32 + l, all NB panel columns). Per column: a shuffle
-// reduction of the norm, one cluster barrier, every lane gathers the CTA partials
-// (DSMEM) and computes the reflector redundantly, the dot products are shuffle-
-// reduced, a second barrier, a gather, the rank-1 update -- no __syncthreads at
-// all, and the dependent FP64 chain per column is kept short (GB300's FP64
-// latency is 64 cycles per add/FMA).
-__device__ __forceinline__ double wsum(double v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-  return v;
-}
-
-template <int ROWS>
-__global__ void __launch_bounds__(32) qr_panel_warp_kernel(double2* __restrict__ a, long lda, int m,
-                                                           int j0, int jb,
-                                                           double2* __restrict__ Tout,
-                                                           double2* __restrict__ V, long ldv) {
-  cg::cluster_group cluster = cg::this_cluster();
-  const int rank = (int)cluster.block_rank();
-  const int cs = (int)cluster.num_blocks();
-  const int lane = threadIdx.x;
-  __shared__ double s_nrm;
-  __shared__ double2 s_alpha;
-  __shared__ double2 s_w[NB];
-  __shared__ double2 s_G[NB][NB];
-
-  const int mp = m - j0;
-  const int chunk = (mp + cs - 1) / cs;
-  const int rb = j0 + rank * chunk;
-  const int re = min(m, rb + chunk);
-
-  // panel rows in registers
-  double2 x[ROWS][NB];
-#pragma unroll
-  for (int t = 0; t < ROWS; ++t) {
-    const int i = rb + t * 32 + lane;
-#pragma unroll
-    for (int c = 0; c < NB; ++c)
-      x[t][c] = (i < re && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
-  }
-  double2 taus_l[NB];   // every lane keeps all tau (uniform across lanes)
-
-#pragma unroll
-  for (int jj = 0; jj < NB; ++jj) {
-    if (jj < jb) {
-      const int col = j0 + jj;
-      const int owner = jj / chunk;
-      // ---- norm of the sub-diagonal part of column jj
-      double acc = 0.0;
-#pragma unroll
-      for (int t = 0; t < ROWS; ++t) {
-        const int i = rb + t * 32 + lane;
-        if (i > col && i < re) acc = fma(x[t][jj].x, x[t][jj].x, fma(x[t][jj].y, x[t][jj].y, acc));
-      }
-      acc = wsum(acc);
-      if (lane == 0) s_nrm = acc;
-      if (rank == owner) {
-        const int lr = col - rb;
-#pragma unroll
-        for (int t = 0; t < ROWS; ++t)
-          if (lr - t * 32 == lane) s_alpha = x[t][jj];
-      }
-      cluster.sync();
-      double v = (lane < cs) ? *cluster.map_shared_rank(&s_nrm, lane) : 0.0;
-      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
-      const double xn2 = wsum(v);
-      // ---- reflector (zlarfg), computed by every lane
-      double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
-      double beta = 0.0;
-      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
-      if (apply) {
-        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
-        const double ib = 1.0 / beta;
-        tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
-        scal = crecip(c2(alpha.x - beta, alpha.y));
-      }
-      taus_l[jj] = tau;
-      // ---- scale own rows below the diagonal, set the diagonal
-#pragma unroll
-      for (int t = 0; t < ROWS; ++t) {
-        const int i = rb + t * 32 + lane;
-        if (apply && i > col && i < re) x[t][jj] = cmul(x[t][jj], scal);
-        if (apply && i == col) x[t][jj] = c2(beta, 0.0);
-      }
-      // ---- w_c = v^H a_c for the remaining panel columns (v_col = 1)
-      double2 w[NB];
-#pragma unroll
-      for (int c = 0; c < NB; ++c) w[c] = c2(0.0, 0.0);
-#pragma unroll
-      for (int t = 0; t < ROWS; ++t) {
-        const int i = rb + t * 32 + lane;
-        if (apply && i >= col && i < re) {
-          const double2 vc = (i == col) ? c2(1.0, 0.0) : cconj(x[t][jj]);
-#pragma unroll
-          for (int c = 0; c < NB; ++c)
-            if (c > jj) w[c] = cfma(vc, x[t][c], w[c]);
-        }
-      }
-#pragma unroll
-      for (int c = 0; c < NB; ++c) {
-        if (c > jj) {
-          w[c].x = wsum(w[c].x);
-          w[c].y = wsum(w[c].y);
-        }
-      }
-      if (lane < NB) {
-        double2 mine = c2(0.0, 0.0);
-#pragma unroll
-        for (int c = 0; c < NB; ++c)
-          if (c == lane) mine = w[c];
-        s_w[lane] = mine;
-      }
-      cluster.sync();
-      // ---- gather the CTA partials: lane c sums rank by rank (same order in every CTA)
-      double2 wc = c2(0.0, 0.0);
-      if (lane < NB && lane > jj) {
-        double2 vals[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r)
-          vals[r] = (r < cs) ? cluster.map_shared_rank(s_w, r)[lane] : c2(0.0, 0.0);
-#pragma unroll
-        for (int h = 8; h > 0; h >>= 1)
-#pragma unroll
-          for (int r = 0; r < h; ++r) vals[r] = cadd(vals[r], vals[r + h]);
-        wc = vals[0];
-      }
-      // ---- rank-1 update of the remaining panel columns
-      const double2 ctau = cconj(tau);
-#pragma unroll
-      for (int c = 0; c < NB; ++c) {
-        if (c > jj) {
-          const double2 wcc = c2(__shfl_sync(0xffffffffu, wc.x, c), __shfl_sync(0xffffffffu, wc.y, c));
-          const double2 f = cmul(ctau, wcc);
-#pragma unroll
-          for (int t = 0; t < ROWS; ++t) {
-            const int i = rb + t * 32 + lane;
-            if (apply && i >= col && i < re) {
-              const double2 vv = (i == col) ? c2(1.0, 0.0) : x[t][jj];
-              x[t][c] = csub(x[t][c], cmul(vv, f));
-            }
-          }
-        }
-      }
-    }
-  }
-
-  // ---- write the panel back and the explicit V
-#pragma unroll
-  for (int t = 0; t < ROWS; ++t) {
-    const int i = rb + t * 32 + lane;
-    if (i < re) {
-#pragma unroll
-      for (int c = 0; c < NB; ++c) {
-        if (c < jb) {
-          const int col = j0 + c;
-          a[(long)i * lda + col] = x[t][c];
-          V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x[t][c];
-        }
-      }
-    }
-  }
-  // ---- partial Gram G[p][c] = v_p^H v_c (p < c) over own rows
-#pragma unroll
-  for (int c = 1; c < NB; ++c) {
-    if (c < jb) {
-      double2 g[NB];
-#pragma unroll
-      for (int p = 0; p < NB; ++p) g[p] = c2(0.0, 0.0);
-#pragma unroll
-      for (int t = 0; t < ROWS; ++t) {
-        const int i = rb + t * 32 + lane;
-        if (i >= j0 + c && i < re) {
-          const double2 vc = (i == j0 + c) ? c2(1.0, 0.0) : x[t][c];
-#pragma unroll
-          for (int p = 0; p < NB; ++p) {
-            if (p < c) {
-              const double2 vp = (i == j0 + p) ? c2(1.0, 0.0) : x[t][p];
-              g[p] = cfma(cconj(vp), vc, g[p]);
-            }
-          }
-        }
-      }
-#pragma unroll
-      for (int p = 0; p < NB; ++p) {
-        if (p < c) {
-          g[p].x = wsum(g[p].x);
-          g[p].y = wsum(g[p].y);
-          if (lane == 0) s_G[p][c] = g[p];
-        }
-      }
-    }
-  }
-  cluster.sync();
-  if (rank == 0) {
-    // lane p gathers column entries p of the summed Gram as they are needed
-    double2 T[NB];   // lane p holds row p of T
-#pragma unroll
-    for (int c = 0; c < NB; ++c) T[c] = c2(0.0, 0.0);
-#pragma unroll
-    for (int c = 0; c < NB; ++c) {
-      if (c < jb) {
-        double2 gpc = c2(0.0, 0.0);
-        if (lane < c) {
-          double2 vals[16];
-#pragma unroll
-          for (int r = 0; r < 16; ++r)
-            vals[r] = (r < cs) ? cluster.map_shared_rank(&s_G[0][0], r)[lane * NB + c] : c2(0.0, 0.0);
-#pragma unroll
-          for (int h = 8; h > 0; h >>= 1)
-#pragma unroll
-            for (int q = 0; q < h; ++q) vals[q] = cadd(vals[q], vals[q + h]);
-          gpc = vals[0];
-        }
-        // T[p][c] = -tau_c sum_{q=p}^{c-1} T[p][q] G[q][c]; G[q][c] lives in lane q
-        double2 acc = c2(0.0, 0.0);
-#pragma unroll
-        for (int q = 0; q < NB; ++q) {
-          if (q < c) {
-            const double2 gqc = c2(__shfl_sync(0xffffffffu, gpc.x, q), __shfl_sync(0xffffffffu, gpc.y, q));
-            if (lane <= q) acc = cfma(T[q], gqc, acc);
-          }
-        }
-        const double2 tc = taus_l[c];
-        if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc);
-        if (lane == c) T[c] = tc;
-      }
-    }
-    if (lane < NB)
-#pragma unroll
-      for (int c = 0; c < NB; ++c) Tout[lane * NB + c] = T[c];
-  }
-  cluster.sync();   // no CTA leaves while its shared memory may still be read
-}
-
-// Panel factorisation for GB300's FP64 budget: a cluster of CS CTAs of 4 warps
-// (one per SM sub-partition, each with its own FP64 pipe), one panel row per
-// thread in registers. Per column: norm and dot products are reduced inside each
-// warp by reduce-scatter (lane l ends up with the warp sum of one value), across
-// the 4 warps through shared memory and across the cluster through distributed
-// shared memory, with two cluster barriers. The reflector scalars are computed by
-// every warp from the gathered partials (no broadcast). The dot products of the
-// new reflector with the previous ones (for T) ride along in the same reduction.
+// Panel factorisation for GB300's FP64 budget: a cluster of CTAs of 1..4 warps,
+// one panel row per thread. Per column: norm and dot products are reduced inside
+// each warp by reduce-scatter (lane l ends up with the warp sum of one value),
+// across the warps through shared memory and across the cluster through
+// distributed shared memory, with two cluster barriers. The reflector scalars are
+// computed by every warp from the gathered partials (no broadcast). The dot
+// products of the new reflector with the previous ones (for T) ride along in the
+// same reduction.
 constexpr int QW = 4;   // warps per CTA
 
 // 16 complex values per lane -> lane l holds the warp sum of value qv(l)
@@ -995,12 +759,6 @@ int panel_cluster_size() {
   if (cudaFuncSetAttribute(qr_panel4_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
       cudaSuccess)
     cudaGetLastError();
-  if (cudaFuncSetAttribute(qr_panel_warp_kernel<1>, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                           1) != cudaSuccess)
-    cudaGetLastError();
-  if (cudaFuncSetAttribute(qr_panel_warp_kernel<2>, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                           1) != cudaSuccess)
-    cudaGetLastError();
   for (int c : {16, 8}) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(c);
@@ -1069,25 +827,6 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
       cfg.numAttrs = 1;
       PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel4_kernel, a, lda, m, j0, jb,
                                       w.T + (long)p * NB * NB, w.V, (long)k));
-    } else if (cs > 1 && chunk <= 64) {
-      cudaLaunchConfig_t cfg = {};
-      cfg.gridDim = dim3(cs);
-      cfg.blockDim = dim3(32);
-      cfg.dynamicSmemBytes = 0;
-      cfg.stream = st;
-      cudaLaunchAttribute attr[1];
-      attr[0].id = cudaLaunchAttributeClusterDimension;
-      attr[0].val.clusterDim.x = cs;
-      attr[0].val.clusterDim.y = 1;
-      attr[0].val.clusterDim.z = 1;
-      cfg.attrs = attr;
-      cfg.numAttrs = 1;
-      if (chunk <= 32)
-        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_warp_kernel<1>, a, lda, m, j0, jb,
-                                        w.T + (long)p * NB * NB, w.V, (long)k));
-      else
-        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel_warp_kernel<2>, a, lda, m, j0, jb,
-                                        w.T + (long)p * NB * NB, w.V, (long)k));
     } else if (cs > 1) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs);
