@@ -430,13 +430,14 @@ __global__ void k_predict(KState* st, DepthArgs a, int Dl, int Dr, double dt_abs
   if (a.params == nullptr || st->s.stopped) return;
   const float y = mlpdef::forward_warp(a.params, x);
   if (lane == 0) {
-    int m = (int)ceilf(y * 20.0f) + 1;   // targets are depth / 20; one step of margin
+    int m = (int)ceilf(y * 20.0f);   // targets are depth / 20
     m = max(m, 2);
     st->s.m_target = (m >= numiter) ? 0 : m;
   }
 }
 
-// after step j: at the learned depth, accept it if the residual estimate is small
+// after step j: from the learned depth on, accept the first depth whose residual
+// estimate is small (a prediction one short costs one more check, not the full depth)
 __global__ void k_depth_check(KState* st, int j, double dt_re, double dt_im, double tol) {
   if (st->s.stopped || st->s.m_target != j + 1) return;
   const int m = j + 1;
@@ -455,7 +456,7 @@ __global__ void k_depth_check(KState* st, int j, double dt_re, double dt_im, dou
       st->s.resid = est;
       st->coef_ready = 1;
     } else {
-      st->s.m_target = 0;   // fall back to the full depth
+      st->s.m_target = j + 2;   // check again after the next iteration (up to the full depth)
     }
   }
 }
