@@ -22,6 +22,7 @@
 #include "ptn_common.cuh"
 #include <cooperative_groups.h>
 #include <algorithm>
+#include <mutex>
 
 namespace cg = cooperative_groups;
 
@@ -694,7 +695,7 @@ inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
 struct QrWs {
   double2* V;
   double2* T;
-  double2* part;
+  double2* part;    // block-update partials (the narrow and the look-ahead update never overlap)
 };
 
 QrWs carve_qr(void* ws, int m, int n) {
@@ -783,6 +784,42 @@ int panel_cluster_size() {
 
 }  // namespace
 
+// Side streams for the look-ahead of the factorisation: a small fixed pool, created
+// at the first QR (which runs eagerly, before any graph capture), lowest priority so
+// that the panel on the caller's stream gets its SMs first; a caller's stream maps
+// to one of them by its handle. Fork / join events are per side stream; every use is
+// issued from one host thread in order, so reusing them is safe (a wait takes the
+// event's latest record at the time of the call).
+struct SideStreams {
+  static constexpr int N = 8;
+  cudaStream_t s[N] = {};
+  cudaEvent_t fork[N] = {}, join[N] = {};
+  bool ok = false;
+};
+
+SideStreams& side_streams() {
+  static SideStreams ss;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess) least = 0;
+    bool good = true;
+    for (int i = 0; i < SideStreams::N && good; ++i) {
+      good = cudaStreamCreateWithPriority(&ss.s[i], cudaStreamNonBlocking, least) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ss.fork[i], cudaEventDisableTiming) == cudaSuccess &&
+             cudaEventCreateWithFlags(&ss.join[i], cudaEventDisableTiming) == cudaSuccess;
+    }
+    if (!good) cudaGetLastError();
+    ss.ok = good;
+  });
+  return ss;
+}
+
+int side_index(cudaStream_t st) {
+  const uintptr_t h = reinterpret_cast<uintptr_t>(st);
+  return (int)((h >> 4) % SideStreams::N);
+}
+
 size_t qr_workspace_bytes(int m, int n) {
   const int k = std::min(m, n);
   const int np = (k + NB - 1) / NB;
@@ -803,7 +840,7 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
   const int prof = prof_begin(st, PROF_QR, 2.0 * fq, 16.0 * 3.0 * m * n);
   const int cs_max = panel_cluster_size();
   const int cap = tune(PTN_TUNE_QR_CLUSTER);
-  for (int j0 = 0, p = 0; j0 < k; j0 += NB, ++p) {
+  auto panel = [&](int j0, int p) -> ptn_status {
     const int jb = std::min(NB, k - j0);
     // cluster of the panel: at least 32 rows per CTA (power of two), at most the
     // device's largest cluster and the tuning cap; small panels take few CTAs and so
@@ -847,11 +884,50 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
     }
     PTN_LAUNCH_CHECK();
     note_launches(1);
-    const int nc = n - j0 - jb;
-    if (nc > 0)
-      PTN_TRY(larfb(a, lda, w.V, k, j0, m, j0 + jb, nc, j0, jb, w.T + (long)p * NB * NB, true,
+    return PTN_OK;
+  };
+  // Look-ahead: after panel p, reflector p is applied first to the columns of panel
+  // p + 1 only (caller's stream), then to the remaining trailing columns on a side
+  // stream while panel p + 1 is factorised on the caller's stream: the latency-bound
+  // panel (one cluster) overlaps the throughput-bound update (the other SMs). The
+  // column ranges are disjoint; the side stream joins back before the next narrow
+  // update (whose columns it has just updated) and at the end. Same kernels and the
+  // same arithmetic as without look-ahead.
+  SideStreams& ss = side_streams();
+  const int si = side_index(st);
+  const bool look_ahead = ss.ok && k > NB;
+  bool pending = false;   // side-stream work not yet joined
+  PTN_TRY(panel(0, 0));
+  for (int j0 = 0, p = 0; j0 < k; j0 += NB, ++p) {
+    const int jb = std::min(NB, k - j0);
+    const int nc = n - j0 - jb;                               // trailing columns
+    const int jn = std::min(NB, std::max(0, k - (j0 + jb)));  // next panel's columns
+    if (pending) {
+      PTN_CUDA_TRY(cudaStreamWaitEvent(st, ss.join[si], 0));
+      pending = false;
+    }
+    if (!look_ahead) {
+      if (nc > 0)
+        PTN_TRY(larfb(a, lda, w.V, k, j0, m, j0 + jb, nc, j0, jb, w.T + (long)p * NB * NB, true,
+                      w.part, st));
+      if (jn > 0) PTN_TRY(panel(j0 + jb, p + 1));
+      continue;
+    }
+    if (jn > 0)
+      PTN_TRY(larfb(a, lda, w.V, k, j0, m, j0 + jb, jn, j0, jb, w.T + (long)p * NB * NB, true,
                     w.part, st));
+    const int rest = nc - jn;
+    if (rest > 0) {
+      PTN_CUDA_TRY(cudaEventRecord(ss.fork[si], st));
+      PTN_CUDA_TRY(cudaStreamWaitEvent(ss.s[si], ss.fork[si], 0));
+      PTN_TRY(larfb(a, lda, w.V, k, j0, m, j0 + jb + jn, rest, j0, jb, w.T + (long)p * NB * NB,
+                    true, w.part, ss.s[si]));
+      PTN_CUDA_TRY(cudaEventRecord(ss.join[si], ss.s[si]));
+      pending = true;
+    }
+    if (jn > 0) PTN_TRY(panel(j0 + jb, p + 1));
   }
+  if (pending) PTN_CUDA_TRY(cudaStreamWaitEvent(st, ss.join[si], 0));
   const int blocks = std::max(1, std::min(4 * num_sms(), (int)(((long)k * n + 255) / 256)));
   extract_r_kernel<<<blocks, 256, 0, st>>>(a, lda, k, n, r, ldr);
   const int qblocks = std::max(1, std::min(4 * num_sms(), (int)(((long)m * k + 255) / 256)));
