@@ -48,3 +48,22 @@ def test_tuning_knobs_validate_and_round_trip():
     assert L.ptn_tune_set(_lib.TUNE_LARFB_TILE, 9) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_set(7, 1) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES) == 1
+
+
+def test_tuner_buckets_and_knob_context():
+    from pytenet_gb300 import _lib, autotune
+    L = _lib.load()
+    _, psis, meta = batch.ising_batch(6, seed=3)
+    for p, m in zip(psis, meta):
+        b, d, _ = autotune.bucket_of(p)
+        assert d == 2 and b >= max(max(a.shape[0], a.shape[2]) for a in p.a) and b & (b - 1) == 0
+    tuning = {"buckets": {str(autotune.bucket_of(psis[0])[:2]):
+                          {str(_lib.TUNE_LARFB_TILE): 3, str(_lib.TUNE_QR_CLUSTER): 1, "mmb": 64}}}
+    vals = autotune.bucket_values(tuning, psis[0])
+    assert vals["mmb"] == 64
+    before = (L.ptn_tune_get(_lib.TUNE_LARFB_TILE), L.ptn_tune_get(_lib.TUNE_QR_CLUSTER))
+    with autotune.knobs_for(tuning, psis[0]):
+        assert L.ptn_tune_get(_lib.TUNE_LARFB_TILE) == 3
+        assert L.ptn_tune_get(_lib.TUNE_QR_CLUSTER) == 1
+    assert (L.ptn_tune_get(_lib.TUNE_LARFB_TILE), L.ptn_tune_get(_lib.TUNE_QR_CLUSTER)) == before
+    assert autotune.bucket_values(None, psis[0]) == {}
