@@ -407,7 +407,7 @@ def our_arm(a):
         out = {"metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
                "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "c128" if a.form == "fp64" else "split-bf16 (fp32 acc) + fp64 krylov/qr",
+               "dtype": "c128" if a.form == "fp64" else "bf16 5-digit fixed point (exact fp32 acc) + f64",
                "data": "synthetic",
                "config": {"workload": workload_desc(a), "form": a.form, "L": a.L, "D": a.D,
                           "numiter_lanczos": a.m, "delta": delta, "graph": a.graph,

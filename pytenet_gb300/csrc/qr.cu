@@ -794,6 +794,7 @@ struct SideStreams {
   static constexpr int N = 8;
   cudaStream_t s[N] = {};
   cudaEvent_t fork[N] = {}, join[N] = {};
+  int device = -1;   // the device they belong to (the look-ahead is off on others)
   bool ok = false;
 };
 
@@ -810,6 +811,7 @@ SideStreams& side_streams() {
              cudaEventCreateWithFlags(&ss.join[i], cudaEventDisableTiming) == cudaSuccess;
     }
     if (!good) cudaGetLastError();
+    if (cudaGetDevice(&ss.device) != cudaSuccess) good = false;
     ss.ok = good;
   });
   return ss;
@@ -895,7 +897,9 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
   // same arithmetic as without look-ahead.
   SideStreams& ss = side_streams();
   const int si = side_index(st);
-  const bool look_ahead = ss.ok && k > NB;
+  int dev = -1;
+  PTN_CUDA_TRY(cudaGetDevice(&dev));
+  const bool look_ahead = ss.ok && ss.device == dev && k > NB;
   bool pending = false;   // side-stream work not yet joined
   PTN_TRY(panel(0, 0));
   for (int j0 = 0, p = 0; j0 < k; j0 += NB, ++p) {
