@@ -569,7 +569,7 @@ def batch_arm(a):
     out = {"metric": BATCH_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": 1,
            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "c128" if prec == "fp64" else "split-bf16 (fp32 acc) + fp64 krylov/qr",
+           "dtype": "c128" if prec == "fp64" else "bf16 5-digit fixed point (exact fp32 acc) + f64",
            "data": "synthetic",
            "config": {"workload": batch_desc(a), "form": prec, "instances": a.batch_count,
                       "site_updates_per_step": site_updates, "d_caps": dmix,
@@ -706,7 +706,7 @@ def precision_arm(a):
     out = {"metric": PREC_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": 1,
            "steps": a.steps, "warmup": a.acc_steps + warm, "ms_per_step": ms / a.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "split-bf16 (fp32 acc) + fp64 krylov/qr", "data": "synthetic",
+           "dtype": "bf16 5-digit fixed point (exact fp32 acc) + f64", "data": "synthetic",
            "config": {"workload": f"XXZ L={L} D={D} J=1 Delta=0.8 h=-0.1 (seed {a.seed}), "
                                   f"dt=0.02j, numiter_lanczos={m}; TDVP steps timed after "
                                   f"{a.acc_steps} accuracy steps",
