@@ -430,7 +430,9 @@ __global__ void k_predict(KState* st, DepthArgs a, int Dl, int Dr, double dt_abs
   if (a.params == nullptr || st->s.stopped) return;
   const float y = mlpdef::forward_warp(a.params, x);
   if (lane == 0) {
-    int m = (int)ceilf(y * 20.0f);   // targets are depth / 20
+    // targets are depth / 20; rounded to nearest: a depth one short costs a
+    // residual check, not more iterations
+    int m = (int)rintf(y * 20.0f);
     m = max(m, 2);
     st->s.m_target = (m >= numiter) ? 0 : m;
   }
