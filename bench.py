@@ -9,15 +9,19 @@ resident in HBM when the timed region starts; the whole state (site tensors,
 environments, Krylov basis: several GB) is far larger than the 129 MB L2, so no
 explicit L2 flush is needed between steps.
 
-  python bench.py [--gpus N] [--steps K] [--warmup W] [--form learned|mixed|fp64]
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--form learned|mixed|fp64] [--no-graph]
 
 Forms: "fp64" = complex128 everywhere, fixed Lanczos depth (the reference's
-method); "mixed" = split-BF16 tensor-core contractions (exact fixed-point digits,
-FP32 accumulation, FP64 recombination) with FP64 Krylov / QR, fixed depth;
-"learned" (default) = "mixed" plus the learned Lanczos depth (trained MLP,
-residual-guarded early exit, falling back to the full depth).
+method); "mixed" = tensor-core contractions from five fixed-point BF16 digits per
+row-scaled value (exact FP32 accumulation per digit level, FP64 recombination) with
+FP64 Krylov / QR, fixed depth; "learned" (default) = "mixed" plus the learned
+Lanczos depth (trained MLP, residual-guarded early exit, falling back to the full
+depth). Each timed step is replayed as a captured CUDA graph unless --no-graph.
   python bench.py --impl reference ...   # the reference CPU algorithm (NumPy oracle
                                          # port) on this host's cores, same metric
+Other workloads (one JSON line each, not the headline):
+  --workload xxz-d1024     XXZ L=32, D=1024: mixed TDVP against FP64 per step, and DMRG
+  --workload ising-batch   256 independent Ising chains (add --autotune)
 
 Multi-GPU: the sweep does not shard (site i+1 depends on site i), so N GPUs run
 N independent replicas of the workload (weak scaling, no collective on the data
