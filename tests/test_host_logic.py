@@ -119,3 +119,27 @@ def test_no_gpu_means_loud_failure():
                   rng=np.random.default_rng(0))
     with pytest.raises(RuntimeError):
         ptg.tdvp_singlesite(h, psi, 0.1j, 1, numiter_lanczos=3)
+
+
+def test_c_abi_argument_errors_without_gpu():
+    """Shape / argument checks of the C ABI come before any device work and map to
+    PTN_BAD_SHAPE with a message (the reference raises AssertionError there)."""
+    from pytenet_gb300 import _lib
+    L = _lib.load()
+    C = _lib.C
+    null = None
+    # empty matrix
+    assert L.ptn_qr(null, 0, 4, null, 4, null, 4, null, 0, null) == _lib.PTN_BAD_SHAPE
+    assert b"empty" in L.ptn_last_error()
+    # ragged / zero dimensions of the effective Hamiltonian
+    assert L.ptn_heff_apply(null, null, null, null, null, 0, 2, 4, 5, 5, 0, null, 0,
+                            null) == _lib.PTN_BAD_SHAPE
+    assert L.ptn_env_step_left(null, null, null, null, null, 4, 2, 0, 5, 5, 0, null, 0,
+                               null) == _lib.PTN_BAD_SHAPE
+    # unknown transposition code of the GEMM
+    assert L.ptn_zgemm(b"X", b"N", 4, 4, 4, _lib.cval(1), null, 4, 0, null, 4, 0, _lib.cval(0),
+                       null, 4, 0, 1, null, 0, null) == _lib.PTN_BAD_SHAPE
+    assert b"bad op" in L.ptn_last_error()
+    # Python layer: shape errors are AssertionErrors, like the reference's
+    err = _lib.PtnShapeError(_lib.PTN_BAD_SHAPE, "x")
+    assert isinstance(err, AssertionError)
