@@ -355,7 +355,7 @@ def our_arm(a):
         peak_src = "bf16_tflops of measured" if "bf16_tflops" in peaks else "bf16 of fallback"
         achieved = k_fl / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
         unit = "TFLOP/s"
-        kern = "tcgen05 split-BF16 complex GEMM"
+        kern = "tcgen05 BF16-digit complex GEMM (5 digits)"
     else:
         # FP64 tensor (DMMA) peak: measured on this machine's GB300 with a DMMA-only kernel
         peak = 1.047

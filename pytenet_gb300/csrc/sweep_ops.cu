@@ -29,7 +29,7 @@ ptn_status heff_apply_f64(const double2*, const double2*, const double2*, const 
 ptn_status bond_apply_f64(const double2*, const double2*, const double2*, double2*, int, int, int,
                           void*, size_t, const int*, cudaStream_t);
 
-// mixed-precision operator (split-BF16 tcgen05 contractions), see mixed.cu
+// mixed-precision operator (BF16-digit tcgen05 contractions), see mixed.cu
 size_t heff_workspace_bytes_mixed(int Dl, int d, int Dr, int chil, int chir);
 size_t bond_workspace_bytes_mixed(int Dl, int Dr, int chi);
 ptn_status heff_prepare_mixed(const double2* w, const double2* l, const double2* r, int Dl, int d,

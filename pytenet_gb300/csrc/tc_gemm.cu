@@ -1,4 +1,4 @@
-// Split-BF16 complex GEMM on the 5th-generation tensor cores (tcgen05, sm_103a),
+// Complex GEMM from fixed-point BF16 digits on the 5th-generation tensor cores (tcgen05, sm_103a),
 // with FP64-class accuracy from exact fixed-point digit products.
 //
 // A complex product C = op(A) op(B) is computed as one real GEMM:
