@@ -277,6 +277,23 @@ def _vdot_step_right(a, b, r):
     return np.tensordot(t, b.conj(), axes=((1, 2), (1, 2)))
 
 
+def apply_mpo(op, psi):
+    """MPO applied to an MPS (chain_ops.py:215-234): per site
+    tensordot(W, A, (2, 1)) -> (chi_l, s, chi_r, D_l, D_r), transposed to
+    (chi_l, D_l, s, chi_r, D_r) and grouped into (chi_l D_l, s, chi_r D_r); bond
+    quantum numbers flattened pairwise (qnumber_flatten of (op, psi))."""
+    assert np.array_equal(psi.qsite, op.qsite)
+    assert psi.nsites == len(op.a)
+    qbonds = [qnumber_flatten((op.qbonds[i], psi.qbonds[i])) for i in range(psi.nsites + 1)]
+    out = OMPS(psi.qsite, qbonds)
+    for i in range(psi.nsites):
+        a = np.tensordot(op.a[i], psi.a[i], axes=(2, 1)).transpose((0, 3, 1, 2, 4))
+        s = a.shape
+        out.a[i] = a.reshape((s[0] * s[1], s[2], s[3] * s[4]))
+        assert is_qsparse(out.a[i], (out.qbonds[i], out.qsite, -out.qbonds[i + 1]))
+    return out
+
+
 def mps_vdot(chi, psi):
     """<chi|psi> (mps.py:430-450)."""
     assert chi.nsites == psi.nsites

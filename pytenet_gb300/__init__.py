@@ -7,7 +7,7 @@ Drop-in API of the reference package (cmendl/pytenet) for this path:
     contraction_operator_step_left / _right, compute_right_operator_blocks,
     lanczos_iteration, expm_krylov, eigh_krylov, eigh_tridiag,
     block_sparse_qr and the quantum-number helpers,
-    heisenberg_xxz_1d_mpo, ising_1d_mpo, mpo_average, mps_vdot, mps_norm.
+    heisenberg_xxz_1d_mpo, ising_1d_mpo, mpo_average, mps_vdot, mps_norm, apply_mpo.
 Additions: TDVPRun (device-resident run, optional CUDA graph), BatchTDVP /
 tdvp_singlesite_batch (many independent instances on streams), the mixed
 precision form (precision="mixed") and the learned Lanczos depth (learned.py).
@@ -26,7 +26,7 @@ from .block_sparse import block_sparse_qr
 from .chain_ops import (apply_local_hamiltonian, apply_local_bond_contraction,
                         contraction_operator_step_left, contraction_operator_step_right,
                         compute_right_operator_blocks, mpo_average, mpo_inner_product,
-                        mps_vdot, mps_norm)
+                        mps_vdot, mps_norm, apply_mpo)
 from .krylov import lanczos_iteration, expm_krylov, eigh_krylov, eigh_tridiag
 from .tdvp import tdvp_singlesite, TDVPRun
 from .dmrg import dmrg_singlesite

@@ -8,7 +8,7 @@ import numpy as np
 import torch
 
 from . import _lib
-from .device import Workspace, call, empty, lib, ptr, stream_ptr, to_dev, to_host
+from .device import Workspace, call, device, empty, lib, ptr, stream_ptr, to_dev, to_host
 
 __all__ = ["apply_local_hamiltonian", "apply_local_bond_contraction",
            "contraction_operator_step_left", "contraction_operator_step_right",
@@ -175,3 +175,57 @@ def mps_vdot(chi, psi):
 def mps_norm(psi):
     """(pytenet/mps.py:453-457)"""
     return float(np.sqrt(mps_vdot(psi, psi).real))
+
+
+def apply_mpo(op, psi):
+    """MPO applied to an MPS (pytenet/chain_ops.py:215-234), contracted on the GPU:
+    per site out[(chi_l, D_l), s, (chi_r, D_r)] = sum_t W[chi_l, s, t, chi_r] A[D_l, t, D_r]
+    as one complex GEMM over the physical index (operands laid out by device
+    gathers), the grouping of the virtual bonds by a final gather. Bond quantum
+    numbers are the pairwise flattening of (op, psi); returns a host MPS like the
+    reference."""
+    from .mps import MPS
+    from .qnumber import qnumber_flatten, is_qsparse
+    assert np.array_equal(np.asarray(psi.qsite), np.asarray(op.qsite))
+    assert len(psi.a) == len(op.a)
+    n = len(psi.a)
+    qbonds = [qnumber_flatten((np.asarray(op.qbonds[i]), np.asarray(psi.qbonds[i])))
+              for i in range(n + 1)]
+    out = MPS(psi.qsite, qbonds, fill="postpone")
+    L, st = lib(), stream_ptr()
+
+    def gather(src, rows, cols, nr, nc):
+        ro = torch.as_tensor(rows, dtype=torch.int64, device=device())
+        co = torch.as_tensor(cols, dtype=torch.int64, device=device())
+        dst = empty((nr, nc))
+        call(L.ptn_gather, ptr(src), ptr(ro), ptr(co), nr, nc, ptr(dst), st)
+        return dst
+
+    tensors = []
+    for i in range(n):
+        w = to_dev(op.a[i])                                 # (cl, d, d, cr)
+        a = to_dev(psi.a[i])                                # (Dl, d, Dr)
+        cl, d, _, cr = op.a[i].shape
+        Dl, _, Dr = psi.a[i].shape
+        # Wm[(cl, s, cr), t] = W[cl, s, t, cr]
+        ic, isd, ir = np.meshgrid(np.arange(cl), np.arange(d), np.arange(cr), indexing="ij")
+        wrows = (ic * d * d * cr + isd * d * cr + ir).reshape(-1)
+        wm = gather(w, wrows, np.arange(d) * cr, cl * d * cr, d)
+        # At[t, (Dl, Dr)] = A[Dl, t, Dr]
+        il, jr = np.meshgrid(np.arange(Dl), np.arange(Dr), indexing="ij")
+        at = gather(a, np.arange(d) * Dr, (il * d * Dr + jr).reshape(-1), d, Dl * Dr)
+        # X[(cl, s, cr), (Dl, Dr)] = Wm . At
+        x = empty((cl * d * cr, Dl * Dr))
+        _zgemm(b"N", b"N", cl * d * cr, Dl * Dr, d, wm, d, at, Dl * Dr, x, Dl * Dr)
+        # out[(cl, Dl, s), (cr, Dr)] = X[cl, s, cr, Dl, Dr]
+        jc, jl, js = np.meshgrid(np.arange(cl), np.arange(Dl), np.arange(d), indexing="ij")
+        orows = (jc * d * cr * Dl * Dr + js * cr * Dl * Dr + jl * Dr).reshape(-1)
+        kc, kr = np.meshgrid(np.arange(cr), np.arange(Dr), indexing="ij")
+        ocols = (kc * Dl * Dr + kr).reshape(-1)
+        t = gather(x, orows, ocols, cl * Dl * d, cr * Dr)
+        tensors.append(t.view(cl * Dl, d, cr * Dr))
+    out.a = [to_host(t).copy() for t in tensors]
+    for i in range(n):
+        assert is_qsparse(out.a[i], [out.qbonds[i], out.qsite, -out.qbonds[i + 1]]), \
+            "sparsity pattern of MPS tensor does not match quantum numbers"
+    return out

@@ -3,7 +3,7 @@ Generate golden fixtures by running the PyTeNet reference itself with fixed seed
 
 Run in a container where the reference checkout exists:
 
-    PTN_REFERENCE=/root/reference python tests/golden/gen_golden.py
+    PTN_REFERENCE=/root/reference python tests/golden/gen_golden.py [fixture ...]
 
 The reference's own tests draw from unseeded generators, so it ships no golden
 vectors; this script makes them. Every fixture stores the exact inputs that
@@ -250,14 +250,28 @@ def gen_mps_random():
     save("mps_random.npz", **pack_mps("r_", psi), **pack_mps("c_", psi2), **pack_mps("d_", psi3))
 
 
+def gen_apply_mpo():
+    """apply_mpo (chain_ops.py:215-234) with non-trivial quantum numbers: XXZ MPO on
+    a random quantum-number-sparse MPS of total spin 2 (the setup of test_tdvp.py)."""
+    rng = np.random.default_rng(1012)
+    nsites = 6
+    h = ptn.heisenberg_xxz_1d_mpo(nsites, 1.0, 0.8, -0.1)
+    qbonds = [np.array([0])]
+    for _ in range(nsites - 1):
+        qbonds.append(np.sort(np.array([q + h.qsite for q in qbonds[-1]]).reshape(-1)))
+    qbonds.append(np.array([2]))
+    psi = ptn.MPS(h.qsite, qbonds, fill="random", rng=rng)
+    op_psi = ptn.apply_mpo(h, psi)
+    save("apply_mpo.npz", **pack_mpo("h_", h), **pack_mps("p0_", psi), **pack_mps("p1_", op_psi))
+
+
+GENERATORS = {"chain_ops": gen_chain_ops, "krylov": gen_krylov, "block_qr": gen_block_qr,
+              "mpos": gen_mpos, "tdvp_readme": gen_tdvp_readme, "tdvp_qnum": gen_tdvp_qnum,
+              "dmrg": gen_dmrg, "tdvp_xxz_bulk": gen_tdvp_xxz_bulk,
+              "ising_imag": gen_ising_imag, "mps_random": gen_mps_random,
+              "apply_mpo": gen_apply_mpo}
+
 if __name__ == "__main__":
-    gen_chain_ops()
-    gen_krylov()
-    gen_block_qr()
-    gen_mpos()
-    gen_tdvp_readme()
-    gen_tdvp_qnum()
-    gen_dmrg()
-    gen_tdvp_xxz_bulk()
-    gen_ising_imag()
-    gen_mps_random()
+    # all fixtures, or only the ones named on the command line
+    for name in (sys.argv[1:] or list(GENERATORS)):
+        GENERATORS[name]()

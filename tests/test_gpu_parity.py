@@ -309,3 +309,16 @@ def test_run_measurements_on_device(ptg):
     run.download()
     assert abs(e_dev - orc.mpo_average(psi, h)) < 1e-12 * max(1.0, abs(e_dev))
     assert abs(n_dev ** 2 - orc.mps_vdot(psi, psi).real) < 1e-12
+
+
+def test_apply_mpo_golden(ptg):
+    """apply_mpo on the GPU (pytenet/chain_ops.py:215-234) against the reference's
+    output: integer bond quantum numbers bit-exact, tensors to 1e-13."""
+    g = load_golden("apply_mpo.npz")
+    h, p0, p1 = golden_mpo(g, "h_"), golden_mps(g, "p0_"), golden_mps(g, "p1_")
+    out = ptg.apply_mpo(h, as_ptg_mps(ptg, p0))
+    for qa, qb in zip(out.qbonds, p1.qbonds):
+        assert np.array_equal(qa, qb)
+    for x, y in zip(out.a, p1.a):
+        assert x.shape == y.shape
+        assert np.max(np.abs(x - y)) < 1e-13 * max(1.0, np.max(np.abs(y)))

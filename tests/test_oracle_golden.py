@@ -163,3 +163,14 @@ def test_mlp_oracle_gradient_by_finite_differences():
         fd = (np.mean((mlp_oracle.mlp_forward(p + e, X) - T) ** 2) -
               np.mean((mlp_oracle.mlp_forward(p - e, X) - T) ** 2)) / 2e-6
         assert abs(fd - g[idx]) < 1e-6 * max(1.0, abs(g[idx]))
+
+
+def test_apply_mpo_matches_reference():
+    """chain_ops.py:215-234 with quantum numbers: tensors and flattened bond qnumbers."""
+    g = load_golden("apply_mpo.npz")
+    h, p0, p1 = golden_mpo(g, "h_"), golden_mps(g, "p0_"), golden_mps(g, "p1_")
+    out = orc.apply_mpo(h, p0)
+    for qa, qb in zip(out.qbonds, p1.qbonds):
+        assert np.array_equal(qa, qb)
+    for x, y in zip(out.a, p1.a):
+        assert x.shape == y.shape and np.allclose(x, y, rtol=0, atol=1e-14)
