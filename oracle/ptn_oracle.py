@@ -521,3 +521,163 @@ def dmrg_singlesite(op, psi, numsweeps, numiter_lanczos=25):
             psi.a[0], np.array([[[1]]]), psi.qsite, psi.qbonds[:2])
         en_min[k] = en
     return en_min
+
+
+# ---------------------------------------------------------------------------
+# two-site sweeps (the next algorithm after the single-site path) --
+# pytenet/bond_ops.py, pytenet/block_sparse_util.py, pytenet/mps.py,
+# pytenet/tdvp.py:121-220, pytenet/dmrg.py:96-178
+# ---------------------------------------------------------------------------
+
+def retained_bond_indices(s, tol):
+    """Singular values kept: those whose normalised squares, accumulated from the
+    smallest up, exceed tol (bond_ops.py:23-38)."""
+    w = np.linalg.norm(s)
+    if w == 0:
+        return np.array([], dtype=int)
+    s = (s / w) ** 2
+    order = np.argsort(s)
+    s[order] = np.cumsum(s[order])
+    return np.where(s > tol)[0]
+
+
+def block_sparse_svd(a, q0, q1):
+    """SVD per common quantum-number block (block_sparse_util.py:264-330); returns
+    (u, s, v, q) with the intermediate quantum numbers q, rows / columns in the
+    input order."""
+    a = np.asarray(a)
+    q0 = np.asarray(q0)
+    q1 = np.asarray(q1)
+    assert is_qsparse(a, [q0, -q1])
+    qis = common_qnumbers(q0, q1)
+    if len(qis) == 0:
+        assert np.linalg.norm(a) == 0
+        u = np.zeros((a.shape[0], 1), dtype=a.dtype)
+        v = np.zeros((1, a.shape[1]), dtype=a.dtype)
+        if a.shape[0] > 0:
+            u[0, 0] = 1
+        return u, np.zeros(1), v, q0[:1]
+    a, (idx0, q0s), (idx1, q1s) = sort_by_qnumbers(a, q0, q1)
+    kmax = min(a.shape)
+    u = np.zeros((a.shape[0], kmax), dtype=a.dtype)
+    v = np.zeros((kmax, a.shape[1]), dtype=a.dtype)
+    s = np.zeros(kmax)
+    q = np.zeros(kmax, dtype=q0s.dtype)
+    k = 0
+    for qn in qis:
+        rs, cs = _qslice(qn, q0s), _qslice(qn, q1s)
+        ub, sb, vb = np.linalg.svd(a[rs, cs], full_matrices=False)
+        u[rs, k:k + len(sb)] = ub
+        v[k:k + len(sb), cs] = vb
+        s[k:k + len(sb)] = sb
+        q[k:k + len(sb)] = qn
+        k += len(sb)
+    u, v, s, q = u[:, :k], v[:k, :], s[:k], q[:k]
+    if np.any(idx0 - np.arange(len(idx0))):
+        u = u[np.argsort(idx0), :]
+    if np.any(idx1 - np.arange(len(idx1))):
+        v = v[:, np.argsort(idx1)]
+    return u, s, v, q
+
+
+def split_block_sparse_matrix_svd(a, q0, q1, tol):
+    """Block-sparse SVD truncated by retained_bond_indices (block_sparse_util.py:244-258)."""
+    u, s, v, q = block_sparse_svd(a, q0, q1)
+    idx = retained_bond_indices(s, tol)
+    return u[:, idx], s[idx], v[idx, :], q[idx]
+
+
+def mps_split_tensor_svd(a, qsite0, qsite1, qbonds_outer, svd_distr, tol=0):
+    """Split a (b0, d0 d1, b2) tensor into (b0, d0, b1) and (b1, d1, b2) by the
+    truncated block-sparse SVD, singular values to the left or right factor
+    (mps.py:538-568)."""
+    qsite0, qsite1 = np.asarray(qsite0), np.asarray(qsite1)
+    d0, d1 = len(qsite0), len(qsite1)
+    assert d0 * d1 == a.shape[1]
+    s = (a.shape[0], d0, d1, a.shape[2])
+    q0 = qnumber_flatten([qbonds_outer[0], qsite0])
+    q1 = qnumber_flatten([-qsite1, qbonds_outer[1]])
+    a0, sigma, a1, qbond = split_block_sparse_matrix_svd(a.reshape((s[0]*s[1], s[2]*s[3])),
+                                                         q0, q1, tol)
+    a0 = a0.reshape((s[0], s[1], len(sigma)))
+    a1 = a1.reshape((len(sigma), s[2], s[3]))
+    if svd_distr == "left":
+        a0 = a0 * sigma
+    elif svd_distr == "right":
+        a1 = a1 * sigma[:, None, None]
+    elif svd_distr == "sqrt":
+        r = np.sqrt(sigma)
+        a0 = a0 * r
+        a1 = a1 * r[:, None, None]
+    else:
+        raise ValueError('`svd_distr` parameter must be "left", "right" or "sqrt".')
+    return a0, a1, qbond
+
+
+def tdvp_twosite(op, psi, dt, numsteps, numiter_lanczos=25, tol_split=0):
+    """Symmetric two-site TDVP; `psi` is overwritten (bond dimensions may change);
+    returns the initial norm (tdvp.py:121-220)."""
+    n = len(op.a)
+    assert n == psi.nsites and n >= 2
+    nrm = orthonormalize(psi, mode="right")
+    rblocks = compute_right_operator_blocks(psi, op)
+    lblocks = [None] * n
+    lblocks[0] = np.array([[[1]]], dtype=rblocks[0].dtype)
+    _check_rblocks(psi, op, rblocks)
+    h2 = [_mpo_merge_pair(op.a[i], op.a[i+1]) for i in range(n - 1)]
+    for _ in range(numsteps):
+        for i in range(n - 2):
+            a = _site_step(lblocks[i], rblocks[i+1], h2[i], _merge_pair(psi.a[i], psi.a[i+1]),
+                           0.5*dt, numiter_lanczos)
+            psi.a[i], psi.a[i+1], psi.qbonds[i+1] = mps_split_tensor_svd(
+                a, psi.qsite, psi.qsite, (psi.qbonds[i], psi.qbonds[i+2]), "right", tol=tol_split)
+            lblocks[i+1] = env_step_left(psi.a[i], psi.a[i], op.a[i], lblocks[i])
+            psi.a[i+1] = _site_step(lblocks[i+1], rblocks[i+1], op.a[i+1], psi.a[i+1],
+                                    -0.5*dt, numiter_lanczos)
+        i = n - 2
+        a = _site_step(lblocks[i], rblocks[i+1], h2[i], _merge_pair(psi.a[i], psi.a[i+1]),
+                       dt, numiter_lanczos)
+        psi.a[i], psi.a[i+1], psi.qbonds[i+1] = mps_split_tensor_svd(
+            a, psi.qsite, psi.qsite, [psi.qbonds[i], psi.qbonds[i+2]], "left", tol=tol_split)
+        rblocks[i] = env_step_right(psi.a[i+1], psi.a[i+1], op.a[i+1], rblocks[i+1])
+        for i in reversed(range(n - 2)):
+            psi.a[i+1] = _site_step(lblocks[i+1], rblocks[i+1], op.a[i+1], psi.a[i+1],
+                                    -0.5*dt, numiter_lanczos)
+            a = _site_step(lblocks[i], rblocks[i+1], h2[i], _merge_pair(psi.a[i], psi.a[i+1]),
+                           0.5*dt, numiter_lanczos)
+            psi.a[i], psi.a[i+1], psi.qbonds[i+1] = mps_split_tensor_svd(
+                a, psi.qsite, psi.qsite, [psi.qbonds[i], psi.qbonds[i+2]], "left", tol=tol_split)
+            rblocks[i] = env_step_right(psi.a[i+1], psi.a[i+1], op.a[i+1], rblocks[i+1])
+    return nrm
+
+
+def dmrg_twosite(op, psi, numsweeps, numiter_lanczos=25, tol_split=0):
+    """Two-site DMRG; `psi` is overwritten; returns the energy after each sweep
+    (dmrg.py:96-178)."""
+    n = len(op.a)
+    assert n == psi.nsites
+    orthonormalize(psi, mode="right")
+    rblocks = compute_right_operator_blocks(psi, op)
+    lblocks = [None] * n
+    lblocks[0] = np.array([[[1]]], dtype=rblocks[0].dtype)
+    _check_rblocks(psi, op, rblocks)
+    en_min = np.zeros(numsweeps)
+    h2 = [_mpo_merge_pair(op.a[i], op.a[i+1]) for i in range(n - 1)]
+    for k in range(numsweeps):
+        en = 0
+        for i in range(n - 2):
+            en, a = _minimize_local_energy(h2[i], lblocks[i], rblocks[i+1],
+                                           _merge_pair(psi.a[i], psi.a[i+1]), numiter_lanczos)
+            psi.a[i], psi.a[i+1], psi.qbonds[i+1] = mps_split_tensor_svd(
+                a, psi.qsite, psi.qsite, [psi.qbonds[i], psi.qbonds[i+2]], "right", tol=tol_split)
+            lblocks[i+1] = env_step_left(psi.a[i], psi.a[i], op.a[i], lblocks[i])
+        for i in reversed(range(n - 1)):
+            en, a = _minimize_local_energy(h2[i], lblocks[i], rblocks[i+1],
+                                           _merge_pair(psi.a[i], psi.a[i+1]), numiter_lanczos)
+            psi.a[i], psi.a[i+1], psi.qbonds[i+1] = mps_split_tensor_svd(
+                a, psi.qsite, psi.qsite, [psi.qbonds[i], psi.qbonds[i+2]], "left", tol=tol_split)
+            rblocks[i] = env_step_right(psi.a[i+1], psi.a[i+1], op.a[i+1], rblocks[i+1])
+        psi.a[0], _, psi.qbonds[0] = local_orthonormalize_right_qr(
+            psi.a[0], np.array([[[1]]]), psi.qsite, psi.qbonds[:2])
+        en_min[k] = en
+    return en_min

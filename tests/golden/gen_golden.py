@@ -265,11 +265,39 @@ def gen_apply_mpo():
     save("apply_mpo.npz", **pack_mpo("h_", h), **pack_mps("p0_", psi), **pack_mps("p1_", op_psi))
 
 
+def gen_twosite():
+    """Two-site TDVP (tdvp.py:121-220) and DMRG (dmrg.py:96-178) with quantum numbers
+    and SVD truncation: the bond dimensions grow from a small start."""
+    rng = np.random.default_rng(1013)
+    nsites = 8
+    h = ptn.heisenberg_xxz_1d_mpo(nsites, 1.0, 0.8, -0.1)
+    qbonds = [np.array([0])]
+    for _ in range(nsites - 1):
+        qbonds.append(np.sort(np.array([q + h.qsite for q in qbonds[-1]]).reshape(-1)))
+    qbonds.append(np.array([2]))
+    # clamp the bonds to at most 4 entries (same sector structure) so that the
+    # two-site steps have room to grow them
+    qbonds = [q if len(q) <= 4 else q[np.linspace(0, len(q) - 1, 4).astype(int)] for q in qbonds]
+    psi = ptn.MPS(h.qsite, qbonds, fill="random", rng=rng)
+    psi0 = copy.deepcopy(psi)
+    dt, numsteps, m, tol = 0.05 - 0.02j, 2, 6, 1e-8
+    import warnings
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        nrm = ptn.tdvp_twosite(h, psi, dt, numsteps, numiter_lanczos=m, tol_split=tol)
+        psi_d = copy.deepcopy(psi0)
+        en = ptn.dmrg_twosite(h, psi_d, 2, numiter_lanczos=10, tol_split=1e-10)
+    save("twosite.npz", **pack_mpo("h_", h), **pack_mps("p0_", psi0), **pack_mps("p1_", psi),
+         **pack_mps("d1_", psi_d), nrm=np.array(nrm), dt=np.array(dt),
+         numsteps=np.array(numsteps), m=np.array(m), tol=np.array(tol), en=en,
+         v1=psi.to_vector(), e1=np.array(ptn.mpo_average(psi, h)))
+
+
 GENERATORS = {"chain_ops": gen_chain_ops, "krylov": gen_krylov, "block_qr": gen_block_qr,
               "mpos": gen_mpos, "tdvp_readme": gen_tdvp_readme, "tdvp_qnum": gen_tdvp_qnum,
               "dmrg": gen_dmrg, "tdvp_xxz_bulk": gen_tdvp_xxz_bulk,
               "ising_imag": gen_ising_imag, "mps_random": gen_mps_random,
-              "apply_mpo": gen_apply_mpo}
+              "apply_mpo": gen_apply_mpo, "twosite": gen_twosite}
 
 if __name__ == "__main__":
     # all fixtures, or only the ones named on the command line

@@ -174,3 +174,39 @@ def test_apply_mpo_matches_reference():
         assert np.array_equal(qa, qb)
     for x, y in zip(out.a, p1.a):
         assert x.shape == y.shape and np.allclose(x, y, rtol=0, atol=1e-14)
+
+
+def test_twosite_tdvp_and_dmrg_match_reference():
+    """Two-site TDVP (tdvp.py:121-220) and DMRG (dmrg.py:96-178) with quantum numbers
+    and truncated block-sparse SVD: bond dimensions and quantum numbers bit-exact,
+    tensors, norm and energies to 1e-10."""
+    g = load_golden("twosite.npz")
+    h = golden_mpo(g, "h_")
+    psi = golden_mps(g, "p0_")
+    psi_d = golden_mps(g, "p0_")
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        nrm = orc.tdvp_twosite(h, psi, complex(g["dt"]), int(g["numsteps"]), int(g["m"]),
+                               float(g["tol"]))
+        en = orc.dmrg_twosite(h, psi_d, 2, 10, 1e-10)
+    assert abs(nrm - float(g["nrm"])) < 1e-12 * max(1.0, abs(float(g["nrm"])))
+    for name, out in (("p1_", psi), ("d1_", psi_d)):
+        ref = golden_mps(g, name)
+        for qa, qb in zip(out.qbonds, ref.qbonds):
+            assert np.array_equal(qa, qb)
+        for x, y in zip(out.a, ref.a):
+            assert x.shape == y.shape
+            assert np.allclose(x, y, rtol=0, atol=1e-10 * max(1.0, np.max(np.abs(y))))
+    assert np.allclose(en, g["en"], rtol=0, atol=1e-12)
+    assert np.allclose(orc.mps_to_vector(psi), g["v1"], atol=1e-10 * np.max(np.abs(g["v1"])))
+    assert abs(orc.mpo_average(psi, h) - complex(g["e1"])) < 1e-10 * max(1.0, abs(complex(g["e1"])))
+
+
+def test_truncation_rule_matches_reference_semantics():
+    """retained_bond_indices (bond_ops.py:23-38): keep the values whose normalised
+    squares, accumulated from the smallest, exceed tol; zero vector keeps nothing."""
+    s = np.array([1.0, 1e-3, 0.5, 1e-6, 0.0])
+    assert list(orc.retained_bond_indices(s.copy(), 0)) == [0, 1, 2, 3]
+    # (1e-3)^2 / 1.25 accumulated with the smaller ones stays below 1e-5: dropped
+    assert list(orc.retained_bond_indices(s.copy(), 1e-5)) == [0, 2]
+    assert list(orc.retained_bond_indices(np.zeros(3), 0.1)) == []
