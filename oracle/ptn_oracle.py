@@ -681,3 +681,50 @@ def dmrg_twosite(op, psi, numsweeps, numiter_lanczos=25, tol_split=0):
             psi.a[0], np.array([[[1]]]), psi.qsite, psi.qbonds[:2])
         en_min[k] = en
     return en_min
+
+
+def local_orthonormalize_left_svd(a, a_next, qsite, qbonds, tol):
+    """Left-orthonormalise `a` by the truncated block-sparse SVD and absorb
+    sigma v into the next tensor (mps.py, mps_local_orthonormalize_left_svd)."""
+    s = a.shape
+    q0 = qnumber_flatten((qbonds[0], qsite))
+    u, sigma, v, qbond = split_block_sparse_matrix_svd(a.reshape((s[0]*s[1], s[2])), q0,
+                                                       qbonds[1], tol)
+    return u.reshape((s[0], s[1], u.shape[1])), np.tensordot(sigma[:, None] * v, a_next, (1, 0)), qbond
+
+
+def local_orthonormalize_right_svd(a, a_prev, qsite, qbonds, tol):
+    """Right-orthonormalise `a` by the truncated block-sparse SVD and absorb
+    u sigma into the previous tensor (mps.py, mps_local_orthonormalize_right_svd)."""
+    s = a.shape
+    q1 = qnumber_flatten([-np.asarray(qsite), qbonds[1]])
+    u, sigma, v, qbond = split_block_sparse_matrix_svd(a.reshape((s[0], s[1]*s[2])), qbonds[0],
+                                                       q1, tol)
+    return v.reshape((v.shape[0], s[1], s[2])), np.tensordot(a_prev, u * sigma, (2, 0)), qbond
+
+
+def compress_svd(psi, tol, direction="left"):
+    """SVD compression and orthonormalisation of an MPS in place; returns the
+    original norm and the scaling factor of the compression (mps.py:196-236)."""
+    n = psi.nsites
+    if direction == "left":
+        nrm = orthonormalize(psi, mode="right")
+        for i in range(n - 1):
+            psi.a[i], psi.a[i+1], psi.qbonds[i+1] = local_orthonormalize_left_svd(
+                psi.a[i], psi.a[i+1], psi.qsite, psi.qbonds[i:i+2], tol)
+        psi.a[-1], t, psi.qbonds[-1] = local_orthonormalize_left_svd(
+            psi.a[-1], np.array([[[1]]]), psi.qsite, psi.qbonds[-2:], tol)
+        assert t.shape == (1, 1, 1)
+        psi.a[-1] = psi.a[-1] * (t[0, 0, 0] / abs(t[0, 0, 0]))
+        return nrm, abs(t[0, 0, 0])
+    if direction == "right":
+        nrm = orthonormalize(psi, mode="left")
+        for i in reversed(range(1, n)):
+            psi.a[i], psi.a[i-1], psi.qbonds[i] = local_orthonormalize_right_svd(
+                psi.a[i], psi.a[i-1], psi.qsite, psi.qbonds[i:i+2], tol)
+        psi.a[0], t, psi.qbonds[0] = local_orthonormalize_right_svd(
+            psi.a[0], np.array([[[1]]]), psi.qsite, psi.qbonds[:2], tol)
+        assert t.shape == (1, 1, 1)
+        psi.a[0] = psi.a[0] * (t[0, 0, 0] / abs(t[0, 0, 0]))
+        return nrm, abs(t[0, 0, 0])
+    raise ValueError(f'`direction` = {direction} invalid; must be "left" or "right".')

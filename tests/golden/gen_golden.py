@@ -293,11 +293,33 @@ def gen_twosite():
          v1=psi.to_vector(), e1=np.array(ptn.mpo_average(psi, h)))
 
 
+def gen_compress():
+    """MPS.compress(tol, "svd", direction) (mps.py:180-236) on an MPS with quantum
+    numbers whose bonds carry more than the state needs: an MPO applied to a state."""
+    rng = np.random.default_rng(1014)
+    nsites = 7
+    h = ptn.heisenberg_xxz_1d_mpo(nsites, 1.0, 0.8, -0.1)
+    qbonds = [np.array([0])]
+    for _ in range(nsites - 1):
+        qbonds.append(np.sort(np.array([q + h.qsite for q in qbonds[-1]]).reshape(-1)))
+    qbonds.append(np.array([1]))
+    psi = ptn.apply_mpo(h, ptn.MPS(h.qsite, qbonds, fill="random", rng=rng))
+    out = {}
+    out.update(pack_mps("p0_", psi))
+    for direction in ("left", "right"):
+        p = copy.deepcopy(psi)
+        nrm, scale = p.compress(1e-6, mode="svd", direction=direction)
+        out.update(pack_mps(f"{direction}_", p))
+        out[f"{direction}_nrm"] = np.array(nrm)
+        out[f"{direction}_scale"] = np.array(scale)
+    save("compress.npz", **out)
+
+
 GENERATORS = {"chain_ops": gen_chain_ops, "krylov": gen_krylov, "block_qr": gen_block_qr,
               "mpos": gen_mpos, "tdvp_readme": gen_tdvp_readme, "tdvp_qnum": gen_tdvp_qnum,
               "dmrg": gen_dmrg, "tdvp_xxz_bulk": gen_tdvp_xxz_bulk,
               "ising_imag": gen_ising_imag, "mps_random": gen_mps_random,
-              "apply_mpo": gen_apply_mpo, "twosite": gen_twosite}
+              "apply_mpo": gen_apply_mpo, "twosite": gen_twosite, "compress": gen_compress}
 
 if __name__ == "__main__":
     # all fixtures, or only the ones named on the command line

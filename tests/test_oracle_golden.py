@@ -210,3 +210,20 @@ def test_truncation_rule_matches_reference_semantics():
     # (1e-3)^2 / 1.25 accumulated with the smaller ones stays below 1e-5: dropped
     assert list(orc.retained_bond_indices(s.copy(), 1e-5)) == [0, 2]
     assert list(orc.retained_bond_indices(np.zeros(3), 0.1)) == []
+
+
+def test_compress_svd_matches_reference():
+    """MPS.compress(tol, "svd", left / right) (mps.py:180-236): truncated bond
+    dimensions and quantum numbers bit-exact, tensors, norm and scale to 1e-10."""
+    g = load_golden("compress.npz")
+    for direction in ("left", "right"):
+        psi = golden_mps(g, "p0_")
+        nrm, scale = orc.compress_svd(psi, 1e-6, direction)
+        ref = golden_mps(g, f"{direction}_")
+        assert abs(nrm - float(g[f"{direction}_nrm"])) < 1e-12 * abs(float(g[f"{direction}_nrm"]))
+        assert abs(scale - float(g[f"{direction}_scale"])) < 1e-12
+        for qa, qb in zip(psi.qbonds, ref.qbonds):
+            assert np.array_equal(qa, qb)
+        for x, y in zip(psi.a, ref.a):
+            assert x.shape == y.shape
+            assert np.allclose(x, y, rtol=0, atol=1e-10)
