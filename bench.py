@@ -13,12 +13,13 @@ explicit L2 flush is needed between steps.
 
 Forms: "fp64" = complex128 everywhere, fixed Lanczos depth (the reference's
 method); "mixed" = tensor-core contractions from five fixed-point BF16 digits per
-row-scaled value (exact FP32 accumulation per digit level, FP64 recombination) with
-FP64 Krylov / QR, fixed depth; "learned" (default) = "mixed" plus the learned
+row-scaled value (exact integer accumulation of the leading digit levels, FP64
+recombination) with FP64 Krylov / QR, fixed depth; "learned" (default) = "mixed" plus the learned
 Lanczos depth (trained MLP, residual-guarded early exit, falling back to the full
 depth). Each timed step is replayed as a captured CUDA graph unless --no-graph.
-  python bench.py --impl reference ...   # the reference CPU algorithm (NumPy oracle
-                                         # port) on this host's cores, same metric
+  python bench.py --impl reference ...   # the reference CPU algorithm (NumPy restatement
+                                         # pinned to the reference's outputs) on this host's
+                                         # cores: whole time steps of the same chain
 Other workloads (one JSON line each, not the headline):
   --workload xxz-d1024     XXZ L=32, D=1024: mixed TDVP against FP64 per step, and DMRG
   --workload ising-batch   256 independent Ising chains (add --autotune)
@@ -60,8 +61,13 @@ def parse():
     p.add_argument("--m", type=int, default=10)
     p.add_argument("--seed", type=int, default=2026)
     p.add_argument("--e2e-steps", type=int, default=1)
-    p.add_argument("--acc-steps", type=int, default=2)
+    p.add_argument("--acc-steps", type=int, default=3,
+                   help="steps of the mixed form in lockstep with the FP64 form (energy, "
+                        "infidelity, norm drift after each; FP64 steps after the first are "
+                        "timed for vs_fp64)")
     p.add_argument("--cpu-sites", type=int, default=3)
+    p.add_argument("--ref-budget", type=float, default=150.0,
+                   help="--impl reference: seconds of whole time steps to time (at least one)")
     p.add_argument("--no-cpu", action="store_true")
     p.add_argument("--no-accuracy", action="store_true")
     p.add_argument("--no-graph", dest="graph", action="store_false",
@@ -149,32 +155,61 @@ def cpu_sample(a, nsites_sample, rng_seed=7):
 
 
 def reference_arm(a):
-    """--impl reference: the reference's CPU algorithm (NumPy oracle port of
-    pytenet) on this host's cores, same metric and config, bounded sample per step."""
+    """--impl reference: the reference's CPU algorithm -- the NumPy restatement of
+    pytenet's tdvp_singlesite, pinned to outputs of the reference itself -- on this
+    host's cores, same workload, metric and config as our arm. Set-up (right
+    normalisation, right environments) is untimed; every timed step is one whole
+    symmetric TDVP time step (2L-1 site updates) of the L=64 chain. Whole steps
+    take about a minute and a half each on 16 cores, so the arm times as many as
+    fit in --ref-budget seconds (at least one), and prints exactly that count."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    import warnings
+    from oracle import ptn_oracle as orc
     cores = os.cpu_count()
-    for _ in range(a.warmup):
-        cpu_sample(a, 1)
-    secs = []
-    for _ in range(a.steps):
-        s, _ = cpu_sample(a, 1)
-        secs.append(s)
-    sec = float(np.mean(secs))
+    h, _, delta = make_workload(a)
+    rng = np.random.default_rng(a.seed)
+    rng.uniform(0.5, 1.5)   # the Delta draw of make_workload
     b = [min(2 ** min(i, a.L - i), a.D) for i in range(a.L + 1)]
-    cost = [b[i] * b[i + 1] * max(b[i], b[i + 1]) for i in range(a.L)]
-    weights = np.array(cost, float) / float(a.D ** 3)
-    sweep_sec = (2.0 * weights.sum() - weights[-1]) * sec
-    value = (2 * a.L - 1) / sweep_sec
-    sample = (f"per step: 1 bulk site update (D={a.D}, random environments) of the NumPy "
-              f"restatement of pytenet's tdvp_singlesite; site-updates/s from the chain's "
-              f"bond profile (sweep = {2.0 * weights.sum() - weights[-1]:.1f} bulk-site units)")
+    psi = orc.random_mps(h.qsite, [np.zeros(bi, dtype=int) for bi in b], rng)
+    orc.orthonormalize(psi, mode="left")
+    t_setup = time.perf_counter()
+    _, lblocks, rblocks = orc.tdvp_setup(h, psi)
+    t_setup = time.perf_counter() - t_setup
+    # warm-up: BLAS threads and allocator on bulk-sized local steps (the sweep's
+    # state is not touched)
+    wrng = np.random.default_rng(7)
+    w = h.a[a.L // 2]
+    for _ in range(a.warmup):
+        x = orc.crandn((a.D, 2, a.D), wrng)
+        env = orc.crandn((a.D, w.shape[0], a.D), wrng)
+        orc.apply_local_hamiltonian(x, w, env, env)
+    dt = 0.05j
+    secs = []
+    t_all = time.perf_counter()
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        while len(secs) < a.steps:
+            t0 = time.perf_counter()
+            orc.tdvp_step(h, psi, lblocks, rblocks, dt, a.m)
+            secs.append(time.perf_counter() - t0)
+            if time.perf_counter() - t_all + secs[-1] > a.ref_budget:
+                break
+    sec = float(np.mean(secs))
+    value = (2 * a.L - 1) / sec
+    sample = (f"{len(secs)} whole TDVP time step(s) of the L={a.L} D={a.D} chain "
+              f"({2 * a.L - 1} site updates each) of the NumPy restatement of pytenet's "
+              f"tdvp_singlesite, {cores} host cores; {len(secs)} of the {a.steps} requested "
+              f"steps fit the {a.ref_budget:.0f} s budget; set-up (right normalisation and "
+              f"environments, {t_setup:.1f} s) untimed")
     out = {"metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": a.gpus,
-           "steps": a.steps, "warmup": a.warmup, "ms_per_step": sweep_sec * 1e3,
+           "steps": len(secs), "requested_steps": a.steps, "warmup": a.warmup,
+           "ms_per_step": sec * 1e3, "step_seconds": secs,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128",
            "data": "synthetic", "impl": "reference",
-           "config": {"workload": workload_desc(a), "l2": "inputs larger than L2"},
+           "config": {"workload": workload_desc(a), "delta": delta,
+                      "l2": "inputs larger than L2"},
            "cpu_baseline": {"value": value, "unit": "site-updates/s", "cores": cores,
                             "kind": "port", "sample": sample},
            "e2e": {"value": value, "unit": "site-updates/s", "h2d_bytes_per_step": 0,
@@ -249,6 +284,21 @@ def max_over_ranks(ms, device):
 def replica_value(world, site_updates, steps, ms_max):
     """Whole-job site-updates/s of `world` independent replicas (weak scaling)."""
     return world * site_updates * steps / (ms_max / 1e3)
+
+
+def kern_key(form):
+    return "zgemm_dmma" if form == "fp64" else "tc_gemm"
+
+
+def capture_traffic(kernel, D):
+    """Mean dram__bytes_read.sum + dram__bytes_write.sum per launch of `kernel` at
+    bond D from the ncu capture summarised in profiles/traffic.json, or None."""
+    try:
+        rec = json.load(open(os.path.join(ROOT, "profiles", "traffic.json")))
+        e = rec[kernel][str(D)]
+        return float(e["bytes_per_launch"]), e["capture"]
+    except Exception:
+        return None, None
 
 
 def our_arm(a):
@@ -351,8 +401,10 @@ def our_arm(a):
     except Exception:
         pass
     if dominant == 1:
-        peak = peaks.get("bf16_tflops", 1900.0)
-        peak_src = "bf16_tflops of measured" if "bf16_tflops" in peaks else "bf16 of fallback"
+        # the GEMM is timed inside seconds-long steps: the sustained BF16 figure
+        peak = peaks.get("bf16_tflops_sustained", 1700.0)
+        peak_src = ("bf16_tflops_sustained of measured" if "bf16_tflops_sustained" in peaks
+                    else "bf16 sustained of fallback")
         achieved = k_fl / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
         unit = "TFLOP/s"
         kern = "tcgen05 BF16-digit complex GEMM (5 digits)"
@@ -363,21 +415,24 @@ def our_arm(a):
         achieved = k_fl / (k_ms / 1e3) / 1e12 if k_ms > 0 else None
         unit = "TFLOP/s"
         kern = "DMMA complex128 GEMM"
-    # DRAM bytes per launch of the dominant kernel from one ncu capture of the same GEMM
-    # shapes (the L=24, D=512 workload, bulk-site launches 481-482: mean of the two)
-    traffic = 50.0e6 if dominant == 1 and a.D == 512 else None
+    # DRAM bytes per launch of the dominant kernel: from one ncu capture of the same
+    # kernel at the same bulk GEMM shapes, kept under profiles/ (null if none matches)
+    traffic, traffic_src = capture_traffic(kern_key(a.form), a.D)
     roofline = {"bound": "tensor", "kernel": kern, "achieved": achieved, "peak": peak,
                 "unit": unit, "frac": (achieved / peak) if achieved else None, "traffic": traffic,
-                "traffic_unit": "bytes per launch (ncu capture at D=512)" if traffic else None,
+                "traffic_unit": "bytes per launch" if traffic else None,
+                "traffic_source": traffic_src,
+                "digit_product_tflops": (achieved * 15.0) if (achieved and dominant == 1) else None,
                 "peak_source": peak_src, "launches_timed": k_n,
                 "kernel_share_of_step": (k_ms / prof_ms) if prof_ms > 0 else None,
                 "qr_share_of_step": (q_ms / prof_ms) if prof_ms > 0 else None,
                 "flops_per_launch": (k_fl / k_n) if k_n else None, "timings_from": prof_from}
 
-    # ---- accuracy of the mixed form vs the FP64 form (same initial state)
-    accuracy = None
+    # ---- accuracy of the mixed form vs the FP64 form (same initial state), and
+    # the FP64 form's own rate on the same chain
+    accuracy, fp64 = None, None
     if a.form != "fp64" and not a.no_accuracy and rank == 0:
-        accuracy = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model)
+        accuracy, fp64 = accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model)
 
     # ---- e2e through the public API with host buffers
     e2e = None
@@ -411,7 +466,7 @@ def our_arm(a):
         out = {"metric": METRIC, "value": value, "unit": "site-updates/s", "n_gpus": world,
                "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-               "dtype": "c128" if a.form == "fp64" else "bf16 5-digit fixed point (exact fp32 acc) + f64",
+               "dtype": "c128" if a.form == "fp64" else "bf16 digits (5 x 8-bit fixed point, tcgen05) + f64",
                "data": "synthetic",
                "config": {"workload": workload_desc(a), "form": a.form, "L": a.L, "D": a.D,
                           "numiter_lanczos": a.m, "delta": delta, "graph": a.graph,
@@ -419,7 +474,10 @@ def our_arm(a):
                           "parallelism": f"replicas x{world}",
                           "l2": "inputs larger than L2 (state of several GB per replica)"},
                "krylov": krylov, "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,
-               "cpu_baseline": cpu, "accuracy_vs_fp64": accuracy}
+               "cpu_baseline": cpu, "accuracy_vs_fp64": accuracy,
+               "fp64_value": fp64["value"] if fp64 else None,
+               "vs_fp64": (value / world / fp64["value"]) if fp64 else None,
+               "fp64_form": fp64}
         print(json.dumps(out))
     if world > 1:
         dist.destroy_process_group()
@@ -573,7 +631,7 @@ def batch_arm(a):
     out = {"metric": BATCH_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": 1,
            "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms / a.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "c128" if prec == "fp64" else "bf16 5-digit fixed point (exact fp32 acc) + f64",
+           "dtype": "c128" if prec == "fp64" else "bf16 digits (5 x 8-bit fixed point, tcgen05) + f64",
            "data": "synthetic",
            "config": {"workload": batch_desc(a), "form": prec, "instances": a.batch_count,
                       "site_updates_per_step": site_updates, "d_caps": dmix,
@@ -710,7 +768,7 @@ def precision_arm(a):
     out = {"metric": PREC_METRIC, "value": value, "unit": "site-updates/s", "n_gpus": 1,
            "steps": a.steps, "warmup": a.acc_steps + warm, "ms_per_step": ms / a.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "bf16 5-digit fixed point (exact fp32 acc) + f64", "data": "synthetic",
+           "dtype": "bf16 digits (5 x 8-bit fixed point, tcgen05) + f64", "data": "synthetic",
            "config": {"workload": f"XXZ L={L} D={D} J=1 Delta=0.8 h=-0.1 (seed {a.seed}), "
                                   f"dt=0.02j, numiter_lanczos={m}; TDVP steps timed after "
                                   f"{a.acc_steps} accuracy steps",
@@ -720,31 +778,58 @@ def precision_arm(a):
 
 
 def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
-    """Energy error, infidelity and norm drift of the benchmarked form (mixed, with
-    the learned depth when given) against the plain FP64 fixed-depth form after
-    `--acc-steps` steps from the same initial state."""
-    from pytenet_gb300.chain_ops import mpo_average, mps_vdot
-    out = {}
+    """The benchmarked form (mixed, with the learned depth when given) and the plain
+    FP64 fixed-depth form from the same initial state, stepped in lockstep for
+    --acc-steps steps: after every step the energy error, infidelity and norm
+    drift against the FP64 form, contracted on the device from the runs' resident
+    tensors. The FP64 steps after the first (which captures the CUDA graph) are
+    timed with CUDA events: the FP64 GPU form's site-updates/s on the same chain,
+    the denominator of the metric's "mixed+learned vs FP64" ratio."""
+    import torch
     runs = {}
     for form in ("mixed", "fp64"):
         p = ptg.MPS(h.qsite, qb0, fill="postpone")
         p.a = [x.copy() for x in psi_host0]
-        r = ptg.TDVPRun(h, p, numiter_lanczos=a.m, precision=form,
-                        depth_model=depth_model if form == "mixed" else None,
-                        depth_tol=a.depth_tol)
-        for _ in range(a.acc_steps):
-            r.step(0.05j)
-        r.download()
-        runs[form] = p
-    pm, pf = runs["mixed"], runs["fp64"]
-    e_m, e_f = mpo_average(pm, h).real, mpo_average(pf, h).real
-    ov = mps_vdot(pf, pm)
-    nm2, nf2 = mps_vdot(pm, pm).real, mps_vdot(pf, pf).real
-    out = {"steps": a.acc_steps, "against": "fp64, fixed depth", "energy_fp64": e_f, "energy_mixed": e_m,
-           "energy_rel_err": abs(e_m - e_f) / max(abs(e_f), 1e-300),
-           "infidelity": 1.0 - abs(ov) ** 2 / (nm2 * nf2),
-           "norm_drift": abs(np.sqrt(nm2) - np.sqrt(nf2))}
-    return out
+        runs[form] = ptg.TDVPRun(h, p, numiter_lanczos=a.m, precision=form, graph=a.graph,
+                                 depth_model=depth_model if form == "mixed" else None,
+                                 depth_tol=a.depth_tol)
+    rm, rf = runs["mixed"], runs["fp64"]
+    per_step, fp64_ms = [], []
+    for k in range(a.acc_steps):
+        rm.step(0.05j)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        rf.step(0.05j)
+        e1.record()
+        torch.cuda.synchronize()
+        if k > 0:
+            fp64_ms.append(e0.elapsed_time(e1))
+        em, ef = rm.energy().real, rf.energy().real
+        ov = rm.vdot(rf)
+        nm2, nf2 = rm.vdot(rm).real, rf.vdot(rf).real
+        per_step.append({"step": k + 1, "energy_fp64": ef, "energy_mixed": em,
+                         "energy_rel_err": abs(em - ef) / max(abs(ef), 1e-300),
+                         "infidelity": 1.0 - abs(ov) ** 2 / (nm2 * nf2),
+                         "norm_drift": abs(np.sqrt(nm2) - np.sqrt(nf2))})
+    last = per_step[-1]
+    out = {"steps": a.acc_steps, "against": "fp64, fixed depth", "energy_fp64": last["energy_fp64"],
+           "energy_mixed": last["energy_mixed"], "energy_rel_err": last["energy_rel_err"],
+           "infidelity": last["infidelity"], "norm_drift": last["norm_drift"],
+           "worst_energy_rel_err": max(r["energy_rel_err"] for r in per_step),
+           "worst_infidelity": max(r["infidelity"] for r in per_step),
+           "worst_norm_drift": max(r["norm_drift"] for r in per_step),
+           "per_step": per_step}
+    fp64 = None
+    if fp64_ms:
+        ms = float(np.mean(fp64_ms))
+        fp64 = {"value": (2 * a.L - 1) / (ms / 1e3), "unit": "site-updates/s",
+                "ms_per_step": ms, "steps_timed": len(fp64_ms), "warmup": 1,
+                "graph": a.graph,
+                "what": "plain complex128 form (FP64 DMMA contractions, FP64 Krylov and QR, "
+                        "fixed depth numiter_lanczos) on the same chain and initial state; the "
+                        "first step (graph capture) untimed"}
+    return out, fp64
 
 
 def main():

@@ -67,7 +67,8 @@ typedef struct {
   double nrm;          /* norm of the start vector */
   double beta_next;    /* norm of the residual left after the final iteration */
   double eval0;        /* lowest Ritz value (eigh mode) */
-  double resid;        /* a-posteriori error estimate beta_next * |e_m^T f(T) e_1| * nrm */
+  double resid;        /* relative a-posteriori error estimate beta_m |e_m^T f(T) e_1|
+                          (the estimate of the step's error divided by nrm), in every mode */
   int32_t early_exits; /* cumulative count of accepted learned depths */
   int32_t iters_total; /* cumulative count of Lanczos vectors used (operator applies) */
   float feat[12];      /* features of the current local step (learned depth) */
@@ -135,7 +136,9 @@ ptn_status ptn_heff_apply(const ptn_c128* a, const ptn_c128* w, const ptn_c128* 
  * 2 * Dl * max(d*chir, chil*d) * Dr * 16 bytes above it are rejected with
  * PTN_BAD_SHAPE. All calls share the array: calls that overlap on the GPU race.
  * The first call on a device looks the array up (cudaGetSymbolAddress with that
- * device current); make it before any stream capture. It allocates nothing. */
+ * device current) and caches the address with the device's current context; make
+ * it before any stream capture. A later call under another context (after
+ * cudaDeviceReset) looks it up again. It allocates nothing. */
 #define PTN_HEFF_NOALLOC_BYTES (32u << 20)
 size_t ptn_heff_noalloc_capacity_bytes(void);
 ptn_status ptn_heff_apply_noalloc(const ptn_c128* a, const ptn_c128* w, const ptn_c128* l,

@@ -444,9 +444,9 @@ def _check_rblocks(psi, op, rblocks):
             "sparsity pattern of operator blocks must match quantum numbers"
 
 
-def tdvp_singlesite(op, psi, dt, numsteps, numiter_lanczos=25):
-    """Symmetric single-site TDVP; `psi` is overwritten; returns the initial
-    norm (tdvp.py:26-118)."""
+def tdvp_setup(op, psi):
+    """The set-up of tdvp_singlesite (tdvp.py:45-63): right-normalise `psi`, build
+    the right operator blocks. Returns (nrm, lblocks, rblocks)."""
     n = len(op.a)
     assert n == psi.nsites
     nrm = orthonormalize(psi, mode="right")
@@ -454,34 +454,48 @@ def tdvp_singlesite(op, psi, dt, numsteps, numiter_lanczos=25):
     lblocks = [None] * n
     lblocks[0] = np.array([[[1]]], dtype=rblocks[0].dtype)
     _check_rblocks(psi, op, rblocks)
+    return nrm, lblocks, rblocks
+
+
+def tdvp_step(op, psi, lblocks, rblocks, dt, numiter_lanczos):
+    """One symmetric time step of tdvp_singlesite (the body of the loop at
+    tdvp.py:65-115); `psi`, `lblocks` and `rblocks` are updated in place."""
+    n = len(op.a)
+    for i in range(n - 1):
+        psi.a[i] = _site_step(lblocks[i], rblocks[i], op.a[i], psi.a[i], 0.5*dt,
+                              numiter_lanczos)
+        s = psi.a[i].shape
+        q, c, psi.qbonds[i+1] = block_sparse_qr(
+            psi.a[i].reshape((s[0]*s[1], s[2])),
+            qnumber_flatten((psi.qbonds[i], psi.qsite)), psi.qbonds[i+1])
+        psi.a[i] = q.reshape((s[0], s[1], q.shape[1]))
+        lblocks[i+1] = env_step_left(psi.a[i], psi.a[i], op.a[i], lblocks[i])
+        c = _bond_step(lblocks[i+1], rblocks[i], c, -0.5*dt, numiter_lanczos)
+        psi.a[i+1] = np.tensordot(c, psi.a[i+1], (1, 0))
+    i = n - 1
+    psi.a[i] = _site_step(lblocks[i], rblocks[i], op.a[i], psi.a[i], dt, numiter_lanczos)
+    for i in reversed(range(1, n)):
+        psi.a[i] = psi.a[i].transpose((2, 1, 0))
+        s = psi.a[i].shape
+        q, c, qbond = block_sparse_qr(
+            psi.a[i].reshape((s[0]*s[1], s[2])),
+            qnumber_flatten((-psi.qbonds[i+1], psi.qsite)), -psi.qbonds[i])
+        psi.qbonds[i] = -qbond
+        psi.a[i] = q.reshape((s[0], s[1], q.shape[1])).transpose((2, 1, 0))
+        rblocks[i-1] = env_step_right(psi.a[i], psi.a[i], op.a[i], rblocks[i])
+        c = np.transpose(c)
+        c = _bond_step(lblocks[i], rblocks[i-1], c, -0.5*dt, numiter_lanczos)
+        psi.a[i-1] = np.tensordot(psi.a[i-1], c, (2, 0))
+        psi.a[i-1] = _site_step(lblocks[i-1], rblocks[i-1], op.a[i-1], psi.a[i-1],
+                                0.5*dt, numiter_lanczos)
+
+
+def tdvp_singlesite(op, psi, dt, numsteps, numiter_lanczos=25):
+    """Symmetric single-site TDVP; `psi` is overwritten; returns the initial
+    norm (tdvp.py:26-118)."""
+    nrm, lblocks, rblocks = tdvp_setup(op, psi)
     for _ in range(numsteps):
-        for i in range(n - 1):
-            psi.a[i] = _site_step(lblocks[i], rblocks[i], op.a[i], psi.a[i], 0.5*dt,
-                                  numiter_lanczos)
-            s = psi.a[i].shape
-            q, c, psi.qbonds[i+1] = block_sparse_qr(
-                psi.a[i].reshape((s[0]*s[1], s[2])),
-                qnumber_flatten((psi.qbonds[i], psi.qsite)), psi.qbonds[i+1])
-            psi.a[i] = q.reshape((s[0], s[1], q.shape[1]))
-            lblocks[i+1] = env_step_left(psi.a[i], psi.a[i], op.a[i], lblocks[i])
-            c = _bond_step(lblocks[i+1], rblocks[i], c, -0.5*dt, numiter_lanczos)
-            psi.a[i+1] = np.tensordot(c, psi.a[i+1], (1, 0))
-        i = n - 1
-        psi.a[i] = _site_step(lblocks[i], rblocks[i], op.a[i], psi.a[i], dt, numiter_lanczos)
-        for i in reversed(range(1, n)):
-            psi.a[i] = psi.a[i].transpose((2, 1, 0))
-            s = psi.a[i].shape
-            q, c, qbond = block_sparse_qr(
-                psi.a[i].reshape((s[0]*s[1], s[2])),
-                qnumber_flatten((-psi.qbonds[i+1], psi.qsite)), -psi.qbonds[i])
-            psi.qbonds[i] = -qbond
-            psi.a[i] = q.reshape((s[0], s[1], q.shape[1])).transpose((2, 1, 0))
-            rblocks[i-1] = env_step_right(psi.a[i], psi.a[i], op.a[i], rblocks[i])
-            c = np.transpose(c)
-            c = _bond_step(lblocks[i], rblocks[i-1], c, -0.5*dt, numiter_lanczos)
-            psi.a[i-1] = np.tensordot(psi.a[i-1], c, (2, 0))
-            psi.a[i-1] = _site_step(lblocks[i-1], rblocks[i-1], op.a[i-1], psi.a[i-1],
-                                    0.5*dt, numiter_lanczos)
+        tdvp_step(op, psi, lblocks, rblocks, dt, numiter_lanczos)
     return nrm
 
 

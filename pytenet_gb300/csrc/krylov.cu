@@ -338,8 +338,10 @@ __global__ void k_tridiag(KState* st, double dt_re, double dt_im, int mode) {
     __syncwarp();
     if (lane == 0) {
       const ptn_c128 cl = st->s.coef[m - 1];
-      // an accepted learned depth already stored its relative estimate
-      if (!st->coef_ready) st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im);
+      // relative estimate beta_m |c_m| / |v| (the coefficients carry the factor |v|);
+      // an accepted learned depth already stored its own
+      if (!st->coef_ready)
+        st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im) / st->s.nrm;
       st->s.iters_total += m;
     }
     return;
@@ -388,9 +390,10 @@ __global__ void k_tridiag(KState* st, double dt_re, double dt_im, int mode) {
   __syncwarp();
   if (lane == 0) {
     const ptn_c128 cl = st->s.coef[m - 1];
-    // an accepted learned depth already stored its relative estimate
+    // relative estimate beta_m |c_m| / |v| (the coefficients carry the factor |v|);
+    // an accepted learned depth already stored its own
     if (st->s.m_target == 0 || st->s.m_used != st->s.m_target)
-      st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im);
+      st->s.resid = st->s.beta_next * sqrt(cl.re * cl.re + cl.im * cl.im) / st->s.nrm;
     st->s.iters_total += m;
   }
 }

@@ -14,7 +14,9 @@
 // it, so calls that overlap on the GPU (different streams, or different host
 // threads without ordering) race on it. The first call on a device looks the
 // array's device address up (cudaGetSymbolAddress, with that device current) and
-// caches it; make that first call before any stream capture.
+// caches it together with the device's current context; make that first call
+// before any stream capture. A call that finds another context current (after a
+// cudaDeviceReset, say, which reloads the module) looks the address up again.
 #include "ptn_common.cuh"
 #include <algorithm>
 #include <mutex>
@@ -32,11 +34,32 @@ constexpr int kMaxDevices = 64;
 __device__ __align__(256) unsigned char g_heff_scratch[kScratchBytes];
 
 void* g_scratch_addr[kMaxDevices] = {};
+void* g_scratch_ctx[kMaxDevices] = {};   // context the cached address belongs to
 std::mutex g_scratch_mu;
+
+typedef int (*CtxGetCurrentFn)(void**);
+
+// the driver's current context (CUcontext) of the calling thread, or null
+void* current_context() {
+  static CtxGetCurrentFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<CtxGetCurrentFn>(f);
+  });
+  void* ctx = nullptr;
+  if (fn == nullptr || fn(&ctx) != 0) return nullptr;
+  return ctx;
+}
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-// device address of the scratch array on the current device (looked up once per device)
+// device address of the scratch array on the current device: looked up once per
+// device and context (a re-created context reloads the module at a new address)
 ptn_status scratch_address(void** out) {
   int dev = -1;
   PTN_CUDA_TRY(cudaGetDevice(&dev));
@@ -45,10 +68,13 @@ ptn_status scratch_address(void** out) {
     return PTN_UNSUPPORTED;
   }
   std::lock_guard<std::mutex> lk(g_scratch_mu);
-  if (g_scratch_addr[dev] == nullptr) {
+  void* ctx = current_context();
+  if (g_scratch_addr[dev] == nullptr || ctx == nullptr || ctx != g_scratch_ctx[dev]) {
     void* p = nullptr;
     PTN_CUDA_TRY(cudaGetSymbolAddress(&p, g_heff_scratch));
     g_scratch_addr[dev] = p;
+    // the lookup made the device's context current if none was
+    g_scratch_ctx[dev] = current_context();
   }
   *out = g_scratch_addr[dev];
   return PTN_OK;

@@ -11,13 +11,23 @@
 //     over the row) and cut into five signed 8-bit integer digits held exactly in
 //     BF16: x = 2^(e[r]-7) * sum_i 2^(-8 i) d_i, |d_i| <= 128 (Ozaki, Ogita, Oishi
 //     and Rump's error-free splitting, in fixed point per row);
-//   - a digit product is an integer of at most 14 bits, so the products of one
-//     level s = i + j (pairs with s <= 4, fifteen in all) add up exactly in an
-//     FP32 accumulator while the partial sums stay below 2^24 (K per split is
-//     capped); each level has its own accumulator in tensor memory (5 levels x 96
-//     columns of the 512);
-//   - the epilogue combines the levels exactly in integer arithmetic and applies
-//     the row and column scales 2^(eA[m] + eB[n] - 46). Split-K partials are FP64.
+//   - a digit product is an integer of at most 14 bits; the products of one level
+//     s = i + j (pairs with s <= 4, fifteen in all) go to that level's FP32
+//     accumulator in tensor memory (5 levels x 96 columns of the 512).
+// Exactness, whatever the signs of the data:
+//   - levels 0..2 (weights 1, 2^-8, 2^-16 of the leading one) restart every
+//     FLUSH_KB K blocks (320 reals): at most 3 pairs x 2^14 x 320 < 2^24, so
+//     every partial sum is an exactly represented integer. The epilogue warps
+//     drain each period into int64 registers (exact) while the tensor cores go on
+//     with the level 3..4 products of the next K block;
+//   - levels 3..4 (weights 2^-24, 2^-32) accumulate over the whole split of at
+//     most MAX_K_SPLIT = 4096 reals in FP32. Their rounding, even with every
+//     product of one sign and a rounding after every 4 products, stays below
+//     2^-45 K (3e-11 at K = 4096 per split after the split-K sum) relative to
+//     max|row| max|col| K; for data of mixed signs it is far smaller.
+//   - the epilogue combines the int64 sum of levels 0..2 with levels 3..4 in
+//     int64 and applies the row and column scales 2^(eA[m] + eB[n] - 46) with one
+//     rounding to FP64. Split-K partials are FP64.
 // What remains is the truncation after the fifth digit and the dropped level-5
 // products, ~2^-39 of the row maxima: FP64-class for the sweep's purposes.
 //
@@ -25,12 +35,12 @@
 // (one 64-byte swizzle atom of BF16). A pipeline stage is one K block with all
 // five digit planes of both operands (3-D TMA boxes of 32 x 128 x 5 and
 // 32 x 96 x 5, 70 KB), so every plane is fetched once and feeds the 15 digit
-// pairs x 2 MMAs of that K block; 3 stages with full/empty mbarriers. Warp 0 lane 0 issues TMA,
-// warp 1 lane 0 issues tcgen05.mma and tcgen05.commit, warps 2..5 read the four
-// accumulators back with tcgen05.ld (warp w owns TMEM lanes 32*(w%4)..) and write
-// FP64 complex results (or FP64 split-K partials). Every mbarrier wait is bounded:
-// on expiry the kernel records an error code, stops issuing work, lets its copies
-// in flight land and still frees its TMEM.
+// pairs x 2 MMAs of that K block; 3 stages with full/empty mbarriers. Warp 0 lane 0
+// issues TMA, warp 1 lane 0 issues tcgen05.mma and tcgen05.commit, warps 2..9 drain
+// the accumulators with tcgen05.ld (warp w owns TMEM lanes 32*(w%4).. and half of the
+// 96 columns) and write FP64 complex results (or FP64 split-K partials). Every
+// mbarrier wait is bounded: on expiry the kernel records an error code, stops
+// issuing work, lets its copies in flight land and still frees its TMEM.
 #include "ptn_common.cuh"
 #include <cuda.h>
 #include <cuda_bf16.h>
@@ -50,6 +60,8 @@ constexpr int STAGES = 3;
 constexpr int NDIGIT = 5;                 // digits per operand value
 constexpr int NPAIR = 15;                 // digit pairs (i, j) with i + j <= 4
 constexpr int NLEVEL = 5;
+constexpr int EXACT_PAIRS = 6;            // pairs of levels 0..2 (first in the pair tables)
+constexpr int FLUSH_KB = 10;              // K blocks per exact period of levels 0..2
 // operand rows without a non-zero entry carry an exponent below this (the digit
 // converter fills the exponent arrays with 0x80 bytes before its max pass)
 constexpr int EXP_NONE = -2000;
@@ -58,9 +70,13 @@ constexpr int B_TILE = BN * BK * 2;
 constexpr int A_STAGE = NDIGIT * A_TILE;       // all five planes
 constexpr int B_STAGE = NDIGIT * B_TILE;
 constexpr int STAGE_BYTES = A_STAGE + B_STAGE; // 70 KB
-// exact integer sums: at most this many real K entries per split
-constexpr int MAX_K_SPLIT = 2048;
-constexpr int THREADS = 192;
+// real K entries per split: bounds the FP32 rounding of levels 3..4 and keeps the
+// int64 sums of levels 0..2 below 2^63 (at most 13 periods of < 2^40.01 each,
+// times 2^16 at the end: < 2^60)
+constexpr int MAX_K_SPLIT = 4096;
+constexpr int EPI_WARPS = 8;
+constexpr int EPI_COLS = BN / 2;              // columns per epilogue warp (two per lane quadrant)
+constexpr int THREADS = 64 + 32 * EPI_WARPS;
 constexpr int TMEM_USED = NLEVEL * BN;   // 480: one accumulator per level
 constexpr int TMEM_COLS = 512;           // allocation (a power of two)
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;   // + barriers, column exponents
@@ -71,6 +87,9 @@ constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >
                            ((uint32_t)(BM >> 4) << 24);
 static_assert(TMEM_USED <= TMEM_COLS, "tensor memory holds 512 columns");
 static_assert(SMEM_BYTES <= 227 * 1024, "shared memory per CTA");
+// every partial sum of levels 0..2 in a period is an integer below 2^24
+static_assert(3L * (1L << 14) * FLUSH_KB * BK < (1L << 24), "exact period of levels 0..2");
+static_assert(MAX_K_SPLIT % BK == 0 && EPI_COLS % 16 == 0, "tiling");
 
 struct TcArgs {
   int M, N;            // output rows, real output columns (2 x complex columns)
@@ -125,6 +144,24 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 
+// bounded wait that also gives up once another role raised the CTA's abort flag
+__device__ __forceinline__ bool mbar_wait_or_abort(uint64_t* bar, uint32_t parity,
+                                                   const int* abort_flag) {
+  const uint32_t a = smem_u32(bar);
+  for (long it = 0; it < WAIT_LIMIT; ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (done) return true;
+    if (*(volatile const int*)abort_flag) return false;
+  }
+  return false;
+}
+
 __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* tm, int x, int y, int z,
                                             uint64_t* bar) {
   asm volatile(
@@ -170,30 +207,44 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16]) {
       : "r"(taddr));
 }
 
+// issue one 32-lane x 8-column load from tensor memory (complete at tmem_wait_ld)
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, uint32_t (&v)[8]) {
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]),
+        "=r"(v[7])
+      : "r"(taddr));
+}
+
 __device__ __forceinline__ void tmem_wait_ld() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 // keeps every use of v after the preceding tcgen05.wait::ld: the empty volatile
 // statements stay in order behind it and redefine the registers
-__device__ __forceinline__ void after_wait(uint32_t (&v)[16]) {
+template <int N>
+__device__ __forceinline__ void after_wait(uint32_t (&v)[N]) {
 #pragma unroll
-  for (int i = 0; i < 16; ++i) asm volatile("" : "+r"(v[i]));
+  for (int i = 0; i < N; ++i) asm volatile("" : "+r"(v[i]));
 }
 
-// sum_s 2^(8 (4 - s)) acc_s of five integer-valued FP32 level sums, times 2^sh.
-// Integer arithmetic throughout (the CUDA-core FP64 rate of this part is low): the
-// only FP64 operation is the int64 -> double conversion; the power of two goes
-// into the exponent field directly (ldexp only where that would leave the normal
-// range).
-__device__ __forceinline__ double combine_levels(uint32_t a0, uint32_t a1, uint32_t a2, uint32_t a3,
-                                                 uint32_t a4, int sh) {
-  const long long i0 = __float2ll_rn(__uint_as_float(a0));
-  const long long i1 = __float2ll_rn(__uint_as_float(a1));
-  const long long i2 = __float2ll_rn(__uint_as_float(a2));
-  const long long i3 = __float2ll_rn(__uint_as_float(a3));
-  const long long i4 = __float2ll_rn(__uint_as_float(a4));
-  const long long v = (((i0 * 256 + i1) * 256 + i2) * 256 + i3) * 256 + i4;   // |v| < 2^58
+// one period of levels 0..2 as an exact integer: 2^16 L0 + 2^8 L1 + L2, the L
+// integer-valued FP32 sums below 2^24 (|result| < 2^40.01)
+__device__ __forceinline__ long long exact_levels(uint32_t a0, uint32_t a1, uint32_t a2) {
+  const long long i0 = __float2int_rn(__uint_as_float(a0));
+  const long long i1 = __float2int_rn(__uint_as_float(a1));
+  const long long i2 = __float2int_rn(__uint_as_float(a2));
+  return i0 * 65536LL + i1 * 256LL + i2;
+}
+
+// (2^16 x + 2^8 L3 + L4) 2^sh as FP64: x the int64 sum of the exact periods of
+// levels 0..2, L3 / L4 integer-valued FP32 sums. Integer arithmetic throughout
+// (the CUDA-core FP64 rate of this part is low): the only FP64 operation is the
+// int64 -> double conversion (the one rounding); the power of two goes into the
+// exponent field directly (ldexp only where that would leave the normal range).
+__device__ __forceinline__ double finish_value(long long x, uint32_t a3, uint32_t a4, int sh) {
+  const long long v = x * 65536LL + __float2ll_rn(__uint_as_float(a3)) * 256LL +
+                      __float2ll_rn(__uint_as_float(a4));   // |v| < 2^61
   if (v == 0) return 0.0;
   const double r = (double)v;
   const long long b = __double_as_longlong(r);
@@ -202,6 +253,25 @@ __device__ __forceinline__ double combine_levels(uint32_t a0, uint32_t a1, uint3
   return ldexp(r, sh);
 }
 
+// the MMAs of digit pairs [P0, P1) of one K block (stage addresses a0 / b0); the
+// first pair of a level starts its accumulator when `restart`
+template <int P0, int P1>
+__device__ __forceinline__ void issue_pairs(uint32_t tmem, uint32_t a0, uint32_t b0, bool restart) {
+#pragma unroll
+  for (int pr = P0; pr < P1; ++pr) {
+    const uint32_t acc_col = (uint32_t)(c_pair_l[pr] * BN);
+    const bool first_of_level = restart && (pr == 0 || c_pair_l[pr] != c_pair_l[pr - 1]);
+    const uint32_t ap = a0 + (uint32_t)(c_pair_a[pr] * A_TILE);
+    const uint32_t bp = b0 + (uint32_t)(c_pair_b[pr] * B_TILE);
+#pragma unroll
+    for (int k = 0; k < BK / 16; ++k)
+      umma(tmem + acc_col, sdesc(ap + k * 32), sdesc(bp + k * 32),
+           (first_of_level && k == 0) ? 0u : 1u);
+  }
+}
+
+// 10 warps: two of the SM's four sub-partitions hold three of them, which caps a
+// thread at 168 registers (16K registers per sub-partition)
 __global__ void __launch_bounds__(THREADS, 1)
     tc_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
                    const TcArgs p) {
@@ -213,8 +283,10 @@ __global__ void __launch_bounds__(THREADS, 1)
   uint8_t* sB = smem + STAGES * A_STAGE;
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
   uint64_t* empty = full + STAGES;
-  uint64_t* tfull = empty + STAGES;
-  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfull + 1);
+  uint64_t* tfull = empty + STAGES;   // levels 0..2 of a period are complete
+  uint64_t* tempty = tfull + 1;       // the epilogue has drained levels 0..2
+  uint64_t* tdone = tempty + 1;       // every MMA of the split is complete
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tdone + 1);
   int* abort_flag = reinterpret_cast<int*>(tslot + 1);
   int* s_eb = abort_flag + 1;   // column exponents of this tile (BN / 2 complex columns)
 
@@ -223,8 +295,9 @@ __global__ void __launch_bounds__(THREADS, 1)
   const int split = blockIdx.z;
   const int kb0 = split * p.kb_per_split;
   const int kb1 = min(p.nkb, kb0 + p.kb_per_split);
-  // one pipeline step per K block
+  // one pipeline step per K block; exact periods of FLUSH_KB steps
   const int it0 = kb0, it1 = kb1;
+  const int nper = (it1 > it0) ? (it1 - it0 + FLUSH_KB - 1) / FLUSH_KB : 0;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -232,6 +305,8 @@ __global__ void __launch_bounds__(THREADS, 1)
       mbar_init(&empty[s], 1);
     }
     mbar_init(tfull, 1);
+    mbar_init(tempty, EPI_WARPS);
+    mbar_init(tdone, 1);
     *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
@@ -255,7 +330,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int it = it0, i = 0; it < it1; ++it, ++i) {
       const int s = i % STAGES;
       const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-      if (i >= STAGES && !mbar_wait(&empty[s], ph ^ 1u)) {
+      if (i >= STAGES && !mbar_wait_or_abort(&empty[s], ph ^ 1u, abort_flag)) {
         atomicExch(p.err, 1);
         *(volatile int*)abort_flag = 1;
         break;
@@ -273,39 +348,54 @@ __global__ void __launch_bounds__(THREADS, 1)
     }
   } else if (warp == 1 && lane == 0) {
     // ---------------- MMA issuer
+    // Per K block: the level 0..2 pairs, then the level 3..4 pairs. At the end of
+    // an exact period (or of the split) the level 0..2 MMAs are committed to tfull
+    // before the level 3..4 MMAs are issued; the first K block of the next period
+    // issues its level 3..4 pairs before it waits for the epilogue to release the
+    // level 0..2 columns, so the tensor cores stay busy while they are drained.
     int issued = 0;
     for (int it = it0, i = 0; it < it1; ++it, ++i) {
       const int s = i % STAGES;
       const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-      if (!mbar_wait(&full[s], ph)) {
+      if (!mbar_wait_or_abort(&full[s], ph, abort_flag)) {
         atomicExch(p.err, 2);
         *(volatile int*)abort_flag = 1;
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
-#pragma unroll
-      for (int pr = 0; pr < NPAIR; ++pr) {
-        const uint32_t acc_col = (uint32_t)(c_pair_l[pr] * BN);
-        // the first k block of this split starts each level's accumulator
-        const bool first_of_level = (it == kb0) && (pr == 0 || c_pair_l[pr] != c_pair_l[pr - 1]);
-        const uint32_t ap = a0 + (uint32_t)(c_pair_a[pr] * A_TILE);
-        const uint32_t bp = b0 + (uint32_t)(c_pair_b[pr] * B_TILE);
-#pragma unroll
-        for (int k = 0; k < BK / 16; ++k)
-          umma(tmem + acc_col, sdesc(ap + k * 32), sdesc(bp + k * 32),
-               (first_of_level && k == 0) ? 0u : 1u);
+      const int q = i / FLUSH_KB;
+      const bool period_start = (i % FLUSH_KB) == 0;
+      const bool period_end = ((i + 1) % FLUSH_KB) == 0 || it + 1 == it1;
+      if (period_start && q > 0) {
+        issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, false);
+        if (!mbar_wait_or_abort(tempty, (uint32_t)(q - 1) & 1u, abort_flag)) {
+          atomicExch(p.err, 2);
+          *(volatile int*)abort_flag = 1;
+          umma_commit(&empty[s]);
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, true);
+        if (period_end) umma_commit(tfull);
+      } else {
+        issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, period_start);
+        if (period_end) umma_commit(tfull);
+        issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, i == 0);
       }
       umma_commit(&empty[s]);
       ++issued;
     }
-    if (issued > 0) umma_commit(tfull);
-    else mbar_arrive(tfull);
+    if (issued > 0) umma_commit(tdone);
+    else mbar_arrive(tdone);
   } else if (warp >= 2) {
-    // ---------------- epilogue: 5 level accumulators -> FP64 -> global
-    // exponents first, while the main loop runs: the row's in a register, the
-    // tile's column exponents in shared memory (epilogue warps' named barrier)
+    // ---------------- epilogue: exact periods of levels 0..2 -> int64, then
+    // levels 3..4 -> FP64 -> global. Warp w reads TMEM lanes 32 (w % 4).. and
+    // the columns [h * 48, h * 48 + 48) of every level, h = (w - 2) / 4.
+    // Exponents first, while the main loop runs: the row's in a register, the
+    // tile's column exponents in shared memory (epilogue warps' named barrier).
     const int g = warp & 3;
+    const int h = (warp - 2) >> 2;
     const int row = m0 + 32 * g + lane;
     const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
     if (warp == 2)
@@ -313,39 +403,65 @@ __global__ void __launch_bounds__(THREADS, 1)
         const int col = (n0 >> 1) + c;
         s_eb[c] = (2 * col < p.N) ? p.eb[col] : EXP_NONE - 1;
       }
-    asm volatile("bar.sync 1, 128;" ::: "memory");
-    const bool ok = mbar_wait(tfull, 0);
-    if (!ok) atomicExch(p.err, 3);
+    asm volatile("bar.sync 1, 256;" ::: "memory");
+    const uint32_t tl = tmem + ((uint32_t)(32 * g) << 16) + (uint32_t)(h * EPI_COLS);
+    long long acc[EPI_COLS];
+#pragma unroll
+    for (int j = 0; j < EPI_COLS; ++j) acc[j] = 0;
+    bool ok = true;
+    for (int q = 0; q < nper && ok; ++q) {
+      if (!mbar_wait_or_abort(tfull, (uint32_t)q & 1u, abort_flag)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int c0 = 0; c0 < EPI_COLS; c0 += 8) {
+        uint32_t v0[8], v1[8], v2[8];
+        __syncwarp();
+        tmem_ld8(tl + (uint32_t)c0, v0);
+        tmem_ld8(tl + (uint32_t)(BN + c0), v1);
+        tmem_ld8(tl + (uint32_t)(2 * BN + c0), v2);
+        tmem_wait_ld();
+        after_wait(v0);
+        after_wait(v1);
+        after_wait(v2);
+        if (c0 + 8 == EPI_COLS) {
+          // every level 0..2 column of this warp is in registers: release them
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0) mbar_arrive(tempty);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) acc[c0 + j] += exact_levels(v0[j], v1[j], v2[j]);
+      }
+    }
+    if (ok && nper > 0 && !mbar_wait_or_abort(tdone, 0, abort_flag)) ok = false;
+    if (!ok && !*(volatile int*)abort_flag) atomicExch(p.err, 3);
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    const bool have = ok && (it1 > it0) && !*(volatile int*)abort_flag;
-    const uint32_t tl = tmem + ((uint32_t)(32 * g) << 16);
-    for (int c0 = 0; c0 < BN; c0 += 16) {
-      uint32_t v0[16], v1[16], v2[16], v3[16], v4[16];
+    const bool have = ok && nper > 0 && !*(volatile int*)abort_flag;
+#pragma unroll
+    for (int c0 = 0; c0 < EPI_COLS; c0 += 16) {
+      uint32_t v3[16], v4[16];
       __syncwarp();
-      tmem_ld16(tl + (uint32_t)c0, v0);
-      tmem_ld16(tl + (uint32_t)(BN + c0), v1);
-      tmem_ld16(tl + (uint32_t)(2 * BN + c0), v2);
       tmem_ld16(tl + (uint32_t)(3 * BN + c0), v3);
       tmem_ld16(tl + (uint32_t)(4 * BN + c0), v4);
       tmem_wait_ld();
-      after_wait(v0);
-      after_wait(v1);
-      after_wait(v2);
       after_wait(v3);
       after_wait(v4);
       if (row < p.M) {
 #pragma unroll
         for (int j = 0; j < 16; j += 2) {
-          const int col = n0 + c0 + j;
+          const int cl = h * EPI_COLS + c0 + j;   // column within the tile
+          const int col = n0 + cl;
           if (col >= p.N) break;
           double re = 0.0, im = 0.0;
-          const int eb = s_eb[(c0 + j) >> 1];
+          const int eb = s_eb[cl >> 1];
           if (have && ea > EXP_NONE && eb > EXP_NONE) {
-            // value = (sum_s 2^(8 (4 - s)) acc_s) 2^(ea + eb - 46); the level sums are
-            // integer-valued FP32, combined exactly in int64, one rounding to FP64
+            // value = (sum_s 2^(8 (4 - s)) level_s) 2^(ea + eb - 46), one rounding
             const int sh = ea + eb - 46;
-            re = combine_levels(v0[j], v1[j], v2[j], v3[j], v4[j], sh);
-            im = combine_levels(v0[j + 1], v1[j + 1], v2[j + 1], v3[j + 1], v4[j + 1], sh);
+            re = finish_value(acc[c0 + j], v3[j], v4[j], sh);
+            im = finish_value(acc[c0 + j + 1], v3[j + 1], v4[j + 1], sh);
           }
           if (p.part != nullptr) {
             double2* dst = reinterpret_cast<double2*>(p.part + ((long)split * p.M + row) * p.N + col);
@@ -442,8 +558,8 @@ MapCache& map_cache() {
   return c;
 }
 
-// 3-D map over digit planes [4][rows][Kp] of BF16, logical extent (K, rows, 4),
-// box (BK, box_rows, 5): one load brings a K block of all five planes
+// 3-D map over the NDIGIT digit planes [5][rows][Kp] of BF16, logical extent
+// (K, rows, 5), box (BK, box_rows, 5): one load brings a K block of all five planes
 bool make_map(CUtensorMap* out, const void* ptr, long rows, long K, long Kp, long plane,
               int box_rows) {
   MapKey key{ptr, rows, K, Kp, plane, box_rows};
@@ -489,8 +605,7 @@ int* err_flag() {
 
 }  // namespace
 
-// K splits: at least what exact integer accumulation needs (MAX_K_SPLIT reals per
-// split), at most enough CTAs for twice PTN_TUNE_TC_SPLIT_WAVES waves (one CTA per SM);
+// K splits: at least what the accuracy bound needs (MAX_K_SPLIT reals per split), at most enough CTAs for twice PTN_TUNE_TC_SPLIT_WAVES waves (one CTA per SM);
 // in between, the split count with the fewest waves x (K blocks per CTA + a fixed
 // per-CTA cost of prologue and epilogue, about KB_OVERHEAD K blocks) -- a grid that
 // spills a few CTAs into another wave costs that whole wave.
@@ -525,8 +640,8 @@ size_t tc_gemm_workspace_bytes(int M, int Ncomplex, int Kcomplex) {
 }
 
 // C (M x Nc complex) = A (M x Kc) * B (Kc x Nc) from digit planes:
-//   Aslices: [4][M][Kp] BF16 (plain) with row exponents ea[M],
-//   Bslices: [4][2 Nc][Kp] BF16 (embedded) with exponents eb[Nc]; Kp >= 2 Kc, Kp % 8 == 0.
+//   Aslices: [5][M][Kp] BF16 (plain) with row exponents ea[M],
+//   Bslices: [5][2 Nc][Kp] BF16 (embedded) with exponents eb[Nc]; Kp >= 2 Kc, Kp % 8 == 0.
 ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* Bslices, long bplane,
                    const int* eb, int M, int Nc, int Kc, long Kp, double2* out, long ldm, long ldn,
                    bool accumulate, void* ws, size_t ws_bytes, const int* skip, cudaStream_t st) {
@@ -553,7 +668,7 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* 
   const int gx = (N + BN - 1) / BN, gy = (M + BM - 1) / BM;
   int splits = choose_splits(M, N, a.nkb);
   // a workspace sized under other knob values: fall back to fewer splits, but
-  // never below what exact integer accumulation needs
+  // never below what the accuracy bound needs
   const int min_splits = (a.nkb + MAX_K_SPLIT / BK - 1) / (MAX_K_SPLIT / BK);
   while (splits > min_splits && (size_t)splits * M * N * sizeof(double) > ws_bytes) --splits;
   if (splits > 1 && (size_t)splits * M * N * sizeof(double) > ws_bytes) {

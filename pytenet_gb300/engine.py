@@ -124,31 +124,39 @@ class DeviceMPS:
         self.qbonds[i] = -plan.qinterm
         return c
 
-    def absorb_left(self, c, i):
-        """psi.a[i] = tensordot(c, psi.a[i], (1, 0)) (pytenet/tdvp.py:84)."""
+    def _gemm(self, M, N, K, a, b, out, mixed):
+        """out (M x N) = a (M x K) b (K x N), row-major complex: FP64 DMMA, or with
+        mixed=True the tensor-core digit GEMM (the contraction arithmetic of the
+        mixed form)."""
         L, st = lib(), stream_ptr()
+        if mixed:
+            wsb = L.ptn_zgemm_split_bf16_workspace_bytes(M, N, K)
+            ws = self.gemm_ws.get(wsb)
+            call(L.ptn_zgemm_split_bf16, ptr(a), K, ptr(b), N, ptr(out), N, M, N, K, ptr(ws),
+                 wsb, st)
+            return
+        wsb = L.ptn_zgemm_workspace_bytes(M, N, K, 1)
+        ws = self.gemm_ws.get(wsb)
+        call(L.ptn_zgemm, b"N", b"N", M, N, K, _lib.cval(1), ptr(a), K, 0, ptr(b), N, 0,
+             _lib.cval(0), ptr(out), N, 0, 1, ptr(ws), wsb, st)
+
+    def absorb_left(self, c, i, mixed=False):
+        """psi.a[i] = tensordot(c, psi.a[i], (1, 0)) (pytenet/tdvp.py:84)."""
         K, n = c.shape
         Dl, d, Dr = self.shape[i]
         assert n == Dl
         out = self.tmp[: K * d * Dr]
-        wsb = L.ptn_zgemm_workspace_bytes(K, d * Dr, n, 1)
-        ws = self.gemm_ws.get(wsb)
-        call(L.ptn_zgemm, b"N", b"N", K, d * Dr, n, _lib.cval(1), ptr(c), n, 0, ptr(self.buf[i]),
-             d * Dr, 0, _lib.cval(0), ptr(out), d * Dr, 0, 1, ptr(ws), wsb, st)
+        self._gemm(K, d * Dr, n, c, self.buf[i], out, mixed)
         self.buf[i][: K * d * Dr].copy_(out)
         self.shape[i] = (K, d, Dr)
 
-    def absorb_right(self, c, i):
+    def absorb_right(self, c, i, mixed=False):
         """psi.a[i] = tensordot(psi.a[i], c, (2, 0)) (pytenet/tdvp.py:112)."""
-        L, st = lib(), stream_ptr()
         n, K = c.shape
         Dl, d, Dr = self.shape[i]
         assert n == Dr
         out = self.tmp[: Dl * d * K]
-        wsb = L.ptn_zgemm_workspace_bytes(Dl * d, K, n, 1)
-        ws = self.gemm_ws.get(wsb)
-        call(L.ptn_zgemm, b"N", b"N", Dl * d, K, n, _lib.cval(1), ptr(self.buf[i]), n, 0, ptr(c),
-             K, 0, _lib.cval(0), ptr(out), K, 0, 1, ptr(ws), wsb, st)
+        self._gemm(Dl * d, K, n, self.buf[i], c, out, mixed)
         self.buf[i][: Dl * d * K].copy_(out)
         self.shape[i] = (Dl, d, K)
 
@@ -367,6 +375,14 @@ class Chain(DeviceMPS):
              ptr(self.state), ptr(ws), self.cws_bytes, st)
 
     # ---------------------------------------------------------------- sweeps
+    def mixed_absorb(self, c, i):
+        """Whether absorbing the bond matrix c into site i runs on the tensor cores:
+        the mixed form, with every dimension of the product at least mixed_min_bond."""
+        if self.prec == _lib.PREC_FP64:
+            return False
+        Dl, d, Dr = self.shape[i]
+        return min(c.shape[0], c.shape[1], Dl, Dr) >= self.mixed_min_bond
+
     def tdvp_step(self, dt):
         """One symmetric single-site TDVP time step (pytenet/tdvp.py:65-115)."""
         n = self.nsites
@@ -375,13 +391,13 @@ class Chain(DeviceMPS):
             c = self.qr_left(i)
             self.env_left(i)
             self.bond_expm(c, self.lenv[i + 1], self.renv[i], self.chi[i + 1], -0.5 * dt, site=i)
-            self.absorb_left(c, i + 1)
+            self.absorb_left(c, i + 1, self.mixed_absorb(c, i + 1))
         self.site_expm(n - 1, dt)
         for i in reversed(range(1, n)):
             c = self.qr_right(i)
             self.env_right(i)
             self.bond_expm(c, self.lenv[i], self.renv[i - 1], self.chi[i], -0.5 * dt, site=i - 1)
-            self.absorb_right(c, i - 1)
+            self.absorb_right(c, i - 1, self.mixed_absorb(c, i - 1))
             self.site_expm(i - 1, 0.5 * dt)
 
     def dmrg_sweep(self, en_out, k):
@@ -391,12 +407,12 @@ class Chain(DeviceMPS):
         for i in range(n - 1):
             self.site_eigh(i)
             c = self.qr_left(i)
-            self.absorb_left(c, i + 1)
+            self.absorb_left(c, i + 1, self.mixed_absorb(c, i + 1))
             self.env_left(i)
         for i in reversed(range(1, n)):
             self.site_eigh(i)
             c = self.qr_right(i)
-            self.absorb_right(c, i - 1)
+            self.absorb_right(c, i - 1, self.mixed_absorb(c, i - 1))
             self.env_right(i)
         self.qr_right(0)
         en_out[k:k + 1].copy_(self.krylov_field_f64("eval0"))

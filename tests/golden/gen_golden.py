@@ -3,7 +3,7 @@ Generate golden fixtures by running the PyTeNet reference itself with fixed seed
 
 Run in a container where the reference checkout exists:
 
-    PTN_REFERENCE=/root/reference python tests/golden/gen_golden.py [fixture ...]
+    PTN_REFERENCE=<reference checkout> python tests/golden/gen_golden.py [fixture ...]
 
 The reference's own tests draw from unseeded generators, so it ships no golden
 vectors; this script makes them. Every fixture stores the exact inputs that
@@ -18,8 +18,9 @@ import sys
 import numpy as np
 from scipy.linalg import expm
 
-REF = os.environ.get("PTN_REFERENCE", "/root/reference")
-sys.path.insert(0, REF)
+# the reference checkout to run: PTN_REFERENCE, else an installed `pytenet`
+if os.environ.get("PTN_REFERENCE"):
+    sys.path.insert(0, os.environ["PTN_REFERENCE"])
 import pytenet as ptn  # noqa: E402
 
 OUT = os.path.dirname(os.path.abspath(__file__))
@@ -315,13 +316,81 @@ def gen_compress():
     save("compress.npz", **out)
 
 
+def weighted_site_mpo(qsite, op, weights):
+    """MPO of sum_i weights[i] op_i (bond 2: "not yet placed" / "placed"), zero
+    quantum numbers, in the reference's layout (chil, d, d, chir)."""
+    L, d = len(weights), op.shape[0]
+    ident = np.identity(d)
+    mpo = ptn.MPO(qsite, [[0]] + (L - 1) * [[0, 0]] + [[0]], fill="postpone")
+    for i in range(L):
+        w = np.zeros((2, d, d, 2))
+        w[0, :, :, 0] = ident
+        w[0, :, :, 1] = weights[i] * op
+        w[1, :, :, 1] = ident
+        if i == 0:
+            w = w[:1]
+        if i == L - 1:
+            w = w[:, :, :, 1:]
+        mpo.a[i] = w
+    return mpo
+
+
+def gen_tdvp_xxz_l64():
+    """Plain complex128 at scale: XXZ L=64 (J=1, Delta=0.8, h=-0.1, zero quantum
+    numbers), bonds min(2^min(i, L-i), 256), seeded complex Gaussian entries,
+    left-orthonormalised; real time dt=0.05j, 20 steps of the reference's own
+    tdvp_singlesite (one call per step), numiter_lanczos=10. The state (134 MB)
+    is not stored: its draws are regenerated from the seed (the draw order is
+    pinned by mps_random.npz) and checked against stored checksums; after every
+    step the fixture keeps gauge-invariant fingerprints: energy, norm, the
+    returned norm, two weighted one-site observables and the overlap with the
+    initial state."""
+    import time
+    seed, L, D, dt, numsteps, m = 2064, 64, 256, 0.05j, 20, 10
+    rng = np.random.default_rng(seed)
+    h = ptn.heisenberg_xxz_1d_mpo(L, 1.0, 0.8, -0.1)
+    h.zero_qnumbers()
+    b = [min(2**min(i, L - i), D) for i in range(L + 1)]
+    psi = ptn.MPS(h.qsite, [bi*[0] for bi in b], fill="random", rng=rng)
+    raw_sum = np.array([x.sum() for x in psi.a])
+    raw_first = np.array([x.reshape(-1)[0] for x in psi.a])
+    psi.orthonormalize(mode="left")
+    psi0 = copy.deepcopy(psi)
+    wrng = np.random.default_rng(seed + 1)
+    cz, cx = wrng.uniform(-1, 1, L), wrng.uniform(-1, 1, L)
+    sz = np.array([[0.5, 0.0], [0.0, -0.5]])
+    sx = np.array([[0.0, 0.5], [0.5, 0.0]])
+    mz = weighted_site_mpo(h.qsite, sz, cz)
+    mx = weighted_site_mpo(h.qsite, sx, cx)
+
+    def fingerprint(p):
+        return [ptn.mpo_average(p, h), ptn.mps_norm(p), ptn.mpo_average(p, mz),
+                ptn.mpo_average(p, mx), ptn.mps_vdot(psi0, p)]
+
+    fp = [fingerprint(psi)]
+    nrms = []
+    t0 = time.perf_counter()
+    for k in range(numsteps):
+        nrms.append(ptn.tdvp_singlesite(h, psi, dt, 1, numiter_lanczos=m))
+        fp.append(fingerprint(psi))
+        print(f"step {k + 1}: E={fp[-1][0].real:.15f} |psi|={fp[-1][1]:.15f} "
+              f"({time.perf_counter() - t0:.0f} s)", flush=True)
+    fp = np.array(fp)
+    save("tdvp_xxz_l64.npz", **pack_mpo("h_", h), **pack_mpo("mz_", mz), **pack_mpo("mx_", mx),
+         seed=np.array(seed), bonds=np.array(b), dt=np.array(dt), numsteps=np.array(numsteps),
+         m=np.array(m), raw_sum=raw_sum, raw_first=raw_first, nrms=np.array(nrms),
+         energy=fp[:, 0], norm=fp[:, 1].real, obs_z=fp[:, 2], obs_x=fp[:, 3], overlap0=fp[:, 4])
+
+
 GENERATORS = {"chain_ops": gen_chain_ops, "krylov": gen_krylov, "block_qr": gen_block_qr,
               "mpos": gen_mpos, "tdvp_readme": gen_tdvp_readme, "tdvp_qnum": gen_tdvp_qnum,
               "dmrg": gen_dmrg, "tdvp_xxz_bulk": gen_tdvp_xxz_bulk,
               "ising_imag": gen_ising_imag, "mps_random": gen_mps_random,
-              "apply_mpo": gen_apply_mpo, "twosite": gen_twosite, "compress": gen_compress}
+              "apply_mpo": gen_apply_mpo, "twosite": gen_twosite, "compress": gen_compress,
+              "tdvp_xxz_l64": gen_tdvp_xxz_l64}
 
 if __name__ == "__main__":
-    # all fixtures, or only the ones named on the command line
-    for name in (sys.argv[1:] or list(GENERATORS)):
+    # all fixtures, or only the ones named on the command line (the L=64 one runs
+    # for a quarter of an hour on 8 cores and is made only when named)
+    for name in (sys.argv[1:] or [g for g in GENERATORS if g != "tdvp_xxz_l64"]):
         GENERATORS[name]()

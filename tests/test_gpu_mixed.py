@@ -1,8 +1,9 @@
 """Mixed-precision form (fixed-point BF16 digit products on tcgen05): the
 tensor-core GEMM and the contractions against FP64 / the oracle, and whole sweeps
-against the FP64 form. Five 8-bit digits per row-scaled value and exact integer
-accumulation per digit level leave ~2^-39 of the row maxima: tolerances 1e-10
-relative for single contractions, stated per test for sweeps."""
+against the FP64 form. Five 8-bit digits per row-scaled value, exact integer
+accumulation of digit levels 0..2 and bounded FP32 accumulation of levels 3..4
+leave ~2^-39 of the row maxima: tolerances 1e-10 relative for single
+contractions, stated per test for sweeps."""
 
 import numpy as np
 import pytest
@@ -78,9 +79,60 @@ def test_split_bf16_gemm_zero_rows_and_scales(ptg):
     assert err.max() < 1e-10, err.max()
 
 
+def same_sign_case(kind, M, N, K, rng):
+    """Operands whose real GEMM (plain A times embedded B) has every product of one
+    sign: the worst case for FP32 accumulation of the digit levels."""
+    if kind == "constant":
+        # identical digits in every entry: every level sum grows linearly in K
+        A = np.full((M, K), 0.7123456789 + 0.4567891234j)
+        B = np.full((K, N), 0.9876543211 + 0.0j)
+    elif kind == "positive":
+        A = rng.uniform(0.5, 1.0, (M, K)) + 1j * rng.uniform(0.5, 1.0, (M, K))
+        B = rng.uniform(0.5, 1.0, (K, N)) + 0j
+    elif kind == "psd-env":
+        # a positive-semidefinite Hermitian environment block X X^H (positive X)
+        # against a non-negative site tensor: the shape of an environment step
+        X = rng.uniform(0.0, 1.0, (max(M, K), 8))
+        A = (X @ X.T)[:M, :K] + 0j
+        B = rng.uniform(0.0, 1.0, (K, N)) + 0j
+    elif kind == "dominant":
+        # one dominant element per row next to small same-sign ones
+        A = rng.uniform(0.0, 1e-3, (M, K)) + 0j
+        A[np.arange(M), rng.integers(0, K, M)] = 1.0
+        B = rng.uniform(0.5, 1.0, (K, N)) + 0j
+    else:
+        raise ValueError(kind)
+    return A, B
+
+
+@pytest.mark.parametrize("kind", ["constant", "positive", "psd-env", "dominant"])
+@pytest.mark.parametrize("mnk", [(256, 192, 1024), (200, 160, 5120), (1024, 512, 5120)])
+def test_split_bf16_gemm_same_sign(ptg, kind, mnk):
+    """Exactness does not depend on random signs: with every digit product of one
+    sign (the worst case for the level sums) at K = 2048 and 10240 reals, and at
+    the environment shapes of D = 1024 (K = 5120 complex), the error stays below
+    1e-10 max|A| max|B| K."""
+    M, N, K = mnk
+    rng = np.random.default_rng(M + N + K)
+    A, B = same_sign_case(kind, M, N, K, rng)
+    C = split_gemm(A, B)
+    ref = A @ B
+    scale = np.abs(A).max() * np.abs(B).max() * K
+    err = np.abs(C - ref).max() / scale
+    # and element by element against the row and column maxima
+    rs = np.abs(A).max(axis=1)[:, None] * np.abs(B).max(axis=0)[None, :] * K
+    err_el = (np.abs(C - ref) / np.maximum(rs, 1e-300)).max()
+    print("same-sign gemm", kind, mnk, err, err_el)
+    assert err < 1e-10, err
+    assert err_el < 1e-10, err_el
+
+
 @pytest.mark.parametrize("dims", [(1, 2, 2, 1, 5), (16, 2, 32, 5, 5), (64, 2, 64, 5, 5),
-                                  (130, 2, 97, 4, 5), (256, 2, 256, 5, 5)])
+                                  (130, 2, 97, 4, 5), (256, 2, 256, 5, 5),
+                                  (512, 2, 512, 5, 5)])
 def test_mixed_contractions(ptg, dims):
+    """Every contraction of the mixed form against the oracle, up to the D = 512
+    bulk shapes of the L = 64 chain (Dl = Dr = 512, chi = 5)."""
     Dl, d, Dr, cl, cr = dims
     rng = np.random.default_rng(11 + sum(dims))
     a = orc.crandn((Dl, d, Dr), rng)

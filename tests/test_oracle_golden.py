@@ -227,3 +227,22 @@ def test_compress_svd_matches_reference():
         for x, y in zip(psi.a, ref.a):
             assert x.shape == y.shape
             assert np.allclose(x, y, rtol=0, atol=1e-10)
+
+
+def test_xxz_l64_fixture_input_and_initial_state():
+    """The L=64, D=256 fixture (whole trajectory checked on the GPU): its input is
+    regenerated from the seed with the reference's draw order, bit for bit, and
+    the left-orthonormalised initial state gives the reference's step-0
+    fingerprints (energy, norm, weighted one-site observables)."""
+    g = load_golden("tdvp_xxz_l64.npz")
+    h, mz, mx = golden_mpo(g, "h_"), golden_mpo(g, "mz_"), golden_mpo(g, "mx_")
+    rng = np.random.default_rng(int(g["seed"]))
+    psi = orc.random_mps(h.qsite, [np.zeros(bi, dtype=int) for bi in g["bonds"]], rng)
+    assert np.array_equal(np.array([x.sum() for x in psi.a]), g["raw_sum"])
+    assert np.array_equal(np.array([x.reshape(-1)[0] for x in psi.a]), g["raw_first"])
+    orc.orthonormalize(psi, mode="left")
+    e = orc.mpo_average(psi, h)
+    assert abs(e - g["energy"][0]) < 1e-12 * abs(g["energy"][0])
+    assert abs(orc.mps_norm(psi) - g["norm"][0]) < 1e-12
+    assert abs(orc.mpo_average(psi, mz) - g["obs_z"][0]) < 1e-12 * max(abs(g["obs_z"][0]), 1e-3)
+    assert abs(orc.mpo_average(psi, mx) - g["obs_x"][0]) < 1e-12 * max(abs(g["obs_x"][0]), 1e-3)
