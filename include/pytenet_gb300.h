@@ -302,6 +302,25 @@ ptn_status ptn_scale(const ptn_c128* in, ptn_c128* out, long n, ptn_c128 alpha, 
 ptn_status ptn_transpose_210(const ptn_c128* in, ptn_c128* out, int n0, int n1, int n2,
                              void* stream);
 
+/* -------------------------------------------------------------------- SVD
+ * Thin SVD a = u diag(s) vh of a complex128 matrix (m x n, row-major, leading
+ * dimension lda), k = min(m, n): u is m x k (ldu), s has k entries in decreasing
+ * order, vh is k x n (ldvh). One-sided Jacobi in FP64 on one CTA. Replaces the
+ * numpy.linalg.svd(full_matrices=False) call per quantum-number block of
+ * block_sparse_svd, pytenet/block_sparse_util.py:244-330 (used by the two-site
+ * splits, pytenet/bond_ops.py:41-53 and pytenet/mps.py:538-568). Singular vectors
+ * are fixed up to a phase per singular value, not necessarily LAPACK's phase.
+ * `sweeps` (device int, or NULL) receives the number of Jacobi sweeps used. */
+size_t ptn_svd_workspace_bytes(int m, int n);
+ptn_status ptn_svd(const ptn_c128* a, int m, int n, long lda, ptn_c128* u, long ldu, double* s,
+                   ptn_c128* vh, long ldvh, int* sweeps, void* ws, size_t ws_bytes,
+                   void* stream);
+/* a[i][j] *= s[j] (side 0) or s[i] (side 1) for a rows x cols row-major matrix
+ * with leading dimension ld: distributing singular values onto a split factor
+ * (the svd_distr argument of pytenet/mps.py:538-568). */
+ptn_status ptn_diag_scale(ptn_c128* a, long rows, long cols, long ld, const double* s, int side,
+                          void* stream);
+
 #ifdef __cplusplus
 }
 #endif

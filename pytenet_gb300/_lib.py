@@ -120,6 +120,9 @@ _SIGS = {
     "ptn_mlp_forward": (I, [P, P, I, P, P]),
     "ptn_mlp_grad": (I, [P, P, P, I, P, P, P, S, P]),
     "ptn_mlp_adam": (I, [P, P, P, P, C.c_float, C.c_float, C.c_float, C.c_float, I, P]),
+    "ptn_svd_workspace_bytes": (S, [I, I]),
+    "ptn_svd": (I, [P, I, I, L, P, L, P, P, L, P, P, S, P]),
+    "ptn_diag_scale": (I, [P, L, L, L, P, I, P]),
     "ptn_qr_workspace_bytes": (S, [I, I]),
     "ptn_qr": (I, [P, I, I, P, L, P, L, P, S, P]),
     "ptn_gather": (I, [P, P, P, I, I, P, P]),

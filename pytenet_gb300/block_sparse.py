@@ -1,5 +1,6 @@
 """
-Block-sparse QR on the device: block_sparse_qr of pytenet/block_sparse_util.py:106-180.
+Block-sparse QR and SVD on the device: block_sparse_qr and block_sparse_svd of
+pytenet/block_sparse_util.py:106-180 and :244-330.
 
 The integer plan (qnumber.QRPlan) says which rows / columns form each quantum-
 number block; the device gathers each block into a dense matrix, runs the
@@ -16,7 +17,8 @@ from . import _lib
 from .device import call, empty, lib, ptr, stream_ptr, to_dev, to_host, Workspace
 from .qnumber import qr_plan, is_qsparse
 
-__all__ = ["RowMajor", "ColMajor", "Flip3", "qr_execute", "block_sparse_qr"]
+__all__ = ["RowMajor", "ColMajor", "Flip3", "qr_execute", "block_sparse_qr", "svd_execute",
+           "block_sparse_svd", "split_block_sparse_matrix_svd"]
 
 
 class RowMajor:
@@ -145,3 +147,122 @@ def block_sparse_qr(a, q0, q1):
     if host:
         return to_host(q), to_host(r), plan.qinterm.copy()
     return q, r, plan.qinterm.copy()
+
+
+# --------------------------------------------------------------------------- SVD
+
+class SVDScratch:
+    """Device scratch of the block SVD (grow-only)."""
+
+    def __init__(self):
+        self.ws = Workspace()
+        self.work = Workspace()
+        self.ub = Workspace()
+        self.vb = Workspace()
+
+
+def svd_execute(plan, src, src_view, scratch):
+    """Block SVD on the device following a QRPlan (its blocks are the SVD's: rows and
+    columns of one common quantum number, min(rows, cols) singular values each, in
+    the plan's quantum-number order). Returns device tensors u (m x K), s (K,),
+    vh (K x n) with rows / columns in the input order (block_sparse_util.py:264-330)."""
+    L = lib()
+    st = stream_ptr()
+    m, n = plan.m, plan.n
+    u = empty((m, plan.K))
+    vh = empty((plan.K, n))
+    s = torch.zeros(plan.K, dtype=torch.float64, device="cuda")
+    u.zero_()
+    vh.zero_()
+    if plan.empty:
+        # no common quantum number: u = e_0, s = 0, vh = 0 (block_sparse_util.py:282-289)
+        if m > 0:
+            u.view(-1)[0] = 1.0
+        return u, s, vh
+    uv, vv = RowMajor(plan.K), RowMajor(n)
+    for (rows, cols, k0, kb), (sro, sco, uro, uco, vro, vco) in zip(
+            plan.blocks, _block_maps(plan, src_view, uv, vv)):
+        mb, nb = len(rows), len(cols)
+        work = scratch.work.get(mb * nb * 16)
+        ub = scratch.ub.get(mb * kb * 16)
+        vb = scratch.vb.get(kb * nb * 16)
+        wsb = L.ptn_svd_workspace_bytes(mb, nb)
+        ws = scratch.ws.get(wsb)
+        call(L.ptn_gather, ptr(src), ptr(sro), ptr(sco), mb, nb, ptr(work), st)
+        call(L.ptn_svd, ptr(work), mb, nb, nb, ptr(ub), kb, ptr(s[k0:k0 + kb]), ptr(vb), nb, None,
+             ptr(ws), wsb, st)
+        call(L.ptn_scatter, ptr(ub), kb, ptr(uro), ptr(uco), mb, kb, ptr(u), st)
+        call(L.ptn_scatter, ptr(vb), nb, ptr(vro), ptr(vco), kb, nb, ptr(vh), st)
+    return u, s, vh
+
+
+_SVD_SCRATCH = None
+
+
+def _svd_scratch():
+    global _SVD_SCRATCH
+    if _SVD_SCRATCH is None:
+        _SVD_SCRATCH = SVDScratch()
+    return _SVD_SCRATCH
+
+
+def block_sparse_svd(a, q0, q1):
+    """Drop-in for pytenet.block_sparse_svd (pytenet/block_sparse_util.py:244-330):
+    SVD per common quantum-number block; returns (u, s, v, q). NumPy input gives
+    NumPy results, a complex128 CUDA tensor gives device tensors (q stays on the
+    host). Singular vectors may differ from LAPACK's by a phase per value."""
+    host = not isinstance(a, torch.Tensor)
+    assert a.ndim == 2
+    q0 = np.asarray(q0)
+    q1 = np.asarray(q1)
+    assert len(q0) == a.shape[0] and len(q1) == a.shape[1]
+    assert is_qsparse(a, [q0, -q1])
+    plan = qr_plan(q0, q1)
+    src = to_dev(a)
+    if plan.empty:
+        assert float(torch.linalg.vector_norm(src).item()) == 0.0
+    u, s, vh = svd_execute(plan, src, RowMajor(a.shape[1]), _svd_scratch())
+    q = plan.qinterm.copy()
+    if host:
+        return to_host(u), s.cpu().numpy(), to_host(vh), q
+    return u, s, vh, q
+
+
+def split_block_sparse_matrix_svd(a, q0, q1, tol):
+    """Drop-in for pytenet.split_block_sparse_matrix_svd (pytenet/bond_ops.py:41-53):
+    block-sparse SVD truncated by retained_bond_indices. The truncation is decided
+    on the host from the singular values (integer bookkeeping, exact); the
+    retained columns / rows are gathered on the device."""
+    from .bond_ops import retained_bond_indices
+    host = not isinstance(a, torch.Tensor)
+    u, s, vh, q = block_sparse_svd(to_dev(a) if host else a, q0, q1)
+    s_host = s.cpu().numpy()
+    idx = retained_bond_indices(s_host, tol)
+    u, vh = take_singular(u, vh, idx)
+    s_keep = s_host[idx]
+    q = q[idx]
+    if host:
+        return to_host(u), s_keep, to_host(vh), q
+    return u, torch.from_numpy(np.ascontiguousarray(s_keep)).to(u.device), vh, q
+
+
+def take_singular(u, vh, idx):
+    """u[:, idx] and vh[idx, :], gathered on the device."""
+    L = lib()
+    st = stream_ptr()
+    m, K = u.shape
+    n = vh.shape[1]
+    k = len(idx)
+    ut = empty((m, k))
+    vt = empty((k, n))
+    if k > 0:
+        # the offset arrays stay referenced until the gathers are enqueued: a freed
+        # temporary could be handed to the next upload before the kernel reads it
+        idx64 = np.asarray(idx, np.int64)
+        u_rows = _dev_i64(np.arange(m, dtype=np.int64) * K)
+        u_cols = _dev_i64(idx64)
+        v_rows = _dev_i64(idx64 * n)
+        v_cols = _dev_i64(np.arange(n, dtype=np.int64))
+        call(L.ptn_gather, ptr(u), ptr(u_rows), ptr(u_cols), m, k, ptr(ut), st)
+        call(L.ptn_gather, ptr(vh), ptr(v_rows), ptr(v_cols), k, n, ptr(vt), st)
+    return ut, vt

@@ -143,3 +143,24 @@ def test_c_abi_argument_errors_without_gpu():
     # Python layer: shape errors are AssertionErrors, like the reference's
     err = _lib.PtnShapeError(_lib.PTN_BAD_SHAPE, "x")
     assert isinstance(err, AssertionError)
+
+
+def test_retained_bond_indices_matches_oracle():
+    """Truncation rule of the two-site splits (pytenet/bond_ops.py:23-38), including
+    an all-zero spectrum and exact zeros."""
+    from pytenet_gb300.bond_ops import retained_bond_indices
+    rng = np.random.default_rng(5)
+    cases = [np.zeros(4), np.array([3.0, 0.0, 0.0]), np.array([1.0])]
+    for _ in range(100):
+        cases.append(np.sort(rng.exponential(size=rng.integers(1, 30)))[::-1] ** 4)
+    for s in cases:
+        for tol in (0.0, 1e-14, 1e-10, 1e-6, 1e-2):
+            assert np.array_equal(retained_bond_indices(s, tol), orc.retained_bond_indices(s.copy(), tol))
+
+
+def test_merge_mpo_pair_matches_oracle():
+    from pytenet_gb300.twosite import merge_mpo_pair
+    rng = np.random.default_rng(6)
+    w0 = rng.normal(size=(3, 2, 2, 4))
+    w1 = rng.normal(size=(4, 2, 2, 5))
+    assert np.allclose(merge_mpo_pair(w0, w1), orc._mpo_merge_pair(w0, w1), rtol=0, atol=1e-14)
