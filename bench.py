@@ -14,9 +14,10 @@ explicit L2 flush is needed between steps.
 Forms: "fp64" = complex128 everywhere, fixed Lanczos depth (the reference's
 method); "mixed" = tensor-core contractions from five fixed-point BF16 digits per
 row-scaled value (exact integer accumulation of the leading digit levels, FP64
-recombination) with FP64 Krylov / QR, fixed depth; "learned" (default) = "mixed" plus the learned
-Lanczos depth (trained MLP, residual-guarded early exit, falling back to the full
-depth). Each timed step is replayed as a captured CUDA graph unless --no-graph.
+recombination) with FP64 Krylov / QR, fixed depth; "learned" (default) = "mixed" plus the
+learned Lanczos depth (trained MLP, residual-guarded early exit, falling back to the full
+depth); "residual" = "mixed" with the same residual estimate tested after every iteration
+from depth 2 and no network (the baseline the learned depth is measured against). Each timed step is replayed as a captured CUDA graph unless --no-graph.
   python bench.py --impl reference ...   # the reference CPU algorithm (NumPy restatement
                                          # pinned to the reference's outputs) on this host's
                                          # cores: whole time steps of the same chain
@@ -52,7 +53,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="ours", choices=["ours", "reference"])
     p.add_argument("--form", default=os.environ.get("PTN_BENCH_FORM", "learned"),
-                   choices=["learned", "mixed", "fp64"])
+                   choices=["learned", "residual", "mixed", "fp64"])
     p.add_argument("--depth-tol", type=float, default=1e-10)
     p.add_argument("--tc-split-waves", type=int, default=None,
                    help="PTN_TUNE_TC_SPLIT_WAVES for the run (library default if unset)")
@@ -329,6 +330,8 @@ def our_arm(a):
     if a.form == "learned":
         from pytenet_gb300.learned import DepthModel
         depth_model = DepthModel.load()
+    elif a.form == "residual":
+        depth_model = "residual"
     run = ptg.TDVPRun(h, psi, numiter_lanczos=a.m, precision=prec, graph=a.graph,
                       depth_model=depth_model, depth_tol=a.depth_tol)
     dt = 0.05j
@@ -378,7 +381,7 @@ def our_arm(a):
     krylov = {"local_steps": nlocal, "lanczos_iterations": ks1.iters_total - ks0.iters_total,
               "mean_depth": (ks1.iters_total - ks0.iters_total) / nlocal,
               "early_exits": ks1.early_exits - ks0.early_exits, "full_depth": a.m,
-              "depth_tol": a.depth_tol if a.form == "learned" else None}
+              "depth_tol": a.depth_tol if a.form in ("learned", "residual") else None}
     clk = clocks.stop()
     ms = e0.elapsed_time(e1)
     if prof_ms is None:

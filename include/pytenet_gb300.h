@@ -52,7 +52,7 @@ typedef enum {
 
 typedef struct { double re, im; } ptn_c128;
 
-#define PTN_ABI_VERSION 1
+#define PTN_ABI_VERSION 2
 #define PTN_KRYLOV_MAXITER 64
 
 /* Device-resident state of one Krylov (Lanczos) run. Laid out for direct reads
@@ -245,6 +245,9 @@ typedef struct {
   double* log;           /* device training-record buffer [capacity][PTN_DEPTH_RECORD], or NULL */
   int* log_count;        /* device record counter */
   int log_capacity;
+  int check_from;        /* with params == NULL: > 0 tests the estimate after every iteration
+                            from this depth on (at least 2) with no network, the residual-only
+                            criterion; 0 keeps the fixed depth */
 } ptn_depth_ctx;
 #define PTN_DEPTH_RECORD 64   /* doubles per record: 12 features, alpha[24], beta[24], nrm, dt re/im, m_used */
 ptn_status ptn_expm_site_ex(ptn_c128* a, const ptn_c128* w, const ptn_c128* l, const ptn_c128* r,

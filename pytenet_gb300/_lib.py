@@ -12,7 +12,7 @@ import threading
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libptn_gb300.so")
-ABI_VERSION = 1
+ABI_VERSION = 2
 KRYLOV_MAXITER = 64
 
 PTN_OK, PTN_BAD_SHAPE, PTN_BREAKDOWN, PTN_NAN, PTN_TIMEOUT, PTN_CUDA_ERROR, PTN_UNSUPPORTED = range(7)
@@ -50,7 +50,8 @@ class DepthCtx(C.Structure):
     """Mirror of ptn_depth_ctx."""
     _fields_ = [("params", C.c_void_p), ("history", C.c_void_p), ("slot", C.c_int),
                 ("site", C.c_int), ("nsites", C.c_int), ("kind", C.c_int), ("tol", C.c_double),
-                ("log", C.c_void_p), ("log_count", C.c_void_p), ("log_capacity", C.c_int)]
+                ("log", C.c_void_p), ("log_count", C.c_void_p), ("log_capacity", C.c_int),
+                ("check_from", C.c_int)]
 
 
 DEPTH_RECORD = 64

@@ -430,7 +430,15 @@ __global__ void k_predict(KState* st, DepthArgs a, int Dl, int Dr, double dt_abs
     for (int i = 0; i < 12; ++i) st->s.feat[i] = x[i];
   }
   __syncwarp();
-  if (a.params == nullptr || st->s.stopped) return;
+  if (st->s.stopped) return;
+  if (a.params == nullptr) {
+    // residual-only criterion: the estimate is tested from depth check_from on
+    if (lane == 0 && a.check_from > 0) {
+      const int m = max(a.check_from, 2);
+      st->s.m_target = (m >= numiter) ? 0 : m;
+    }
+    return;
+  }
   const float y = mlpdef::forward_warp(a.params, x);
   if (lane == 0) {
     // targets are depth / 20; rounded to nearest: a depth one short costs a

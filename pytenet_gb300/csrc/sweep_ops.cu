@@ -86,7 +86,7 @@ ptn_status krylov_run(const LocalOp& op, double2* x, double dt_re, double dt_im,
     if (depth != nullptr) {
       if (j == 0)
         PTN_TRY(depth_predict(state, depth, op.Dl, op.Dr, dt_abs, numiter, st));
-      if (depth->params != nullptr && j >= 1)
+      if ((depth->params != nullptr || depth->check_from > 0) && j >= 1)
         PTN_TRY(depth_check(state, j, dt_re, dt_im, depth->tol, st));
     }
   }

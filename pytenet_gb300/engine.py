@@ -189,10 +189,11 @@ class DeviceMPS:
 
 class DepthState:
     """Device buffers of the learned Lanczos depth: per-(site, kind) history of
-    the previous alpha / beta, the MLP parameters (or None: fixed depth), and an
+    the previous alpha / beta, the MLP parameters (or None: fixed depth, or with
+    check_from > 0 the residual-only criterion tested from that depth on), and an
     optional training-record log."""
 
-    def __init__(self, nsites, params=None, tol=1e-10, log_capacity=0):
+    def __init__(self, nsites, params=None, tol=1e-10, log_capacity=0, check_from=0):
         self.history = torch.zeros((2 * nsites, 8), dtype=torch.float32, device=device())
         self.params = params
         self.tol = float(tol)
@@ -204,6 +205,7 @@ class DepthState:
                                    device=device())
             self.log_count = torch.zeros(1, dtype=torch.int32, device=device())
         self.nsites = nsites
+        self.check_from = int(check_from)
 
     def ctx(self, site, kind):
         c = _lib.DepthCtx()
@@ -217,6 +219,7 @@ class DepthState:
         c.log = ptr(self.log) if self.log is not None else None
         c.log_count = ptr(self.log_count) if self.log_count is not None else None
         c.log_capacity = self.log_capacity
+        c.check_from = self.check_from
         return c
 
     def records(self):

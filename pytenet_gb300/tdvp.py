@@ -18,7 +18,8 @@ class TDVPRun:
     contractions on the tensor cores, FP64 Krylov / QR).
     depth_model: a trained learned.DepthModel; numiter_lanczos is then the full
     depth the run falls back to whenever the residual estimate at the predicted
-    depth exceeds depth_tol.
+    depth exceeds depth_tol. depth_model="residual" tests the same estimate after
+    every iteration from depth 2 on, with no network (the residual-only criterion).
     graph: capture one time step in a CUDA graph after the first step and
     replay it (all buffers are preallocated and no step synchronises).
     mixed_min_bond: smallest bond on which the mixed form uses the tensor cores
@@ -32,8 +33,12 @@ class TDVPRun:
         depth = None
         if depth_model is not None or record_capacity > 0:
             from .engine import DepthState
-            params = depth_model.params if depth_model is not None else None
-            depth = DepthState(nsites, params, depth_tol, record_capacity)
+            residual = isinstance(depth_model, str)
+            if residual and depth_model != "residual":
+                raise ValueError('depth_model must be a DepthModel, "residual" or None')
+            params = depth_model.params if (depth_model is not None and not residual) else None
+            depth = DepthState(nsites, params, depth_tol, record_capacity,
+                               check_from=2 if residual else 0)
         self.chain = Chain(hamiltonian, psi, numiter_lanczos, precision, depth=depth,
                            mixed_min_bond=mixed_min_bond)
         # right-normalise, build the environments (pytenet/tdvp.py:51-63)
