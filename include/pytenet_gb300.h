@@ -96,13 +96,19 @@ uint64_t ptn_launch_count(void);
  *                              1 16x16, 2 32x16, 3 32x32, 4 64x32 (rows x columns)
  *   PTN_TUNE_QR_CLUSTER        largest thread-block cluster of the QR panel: 0 the
  *                              device's (default; at least 32 rows per CTA), or 1..16
+ *   PTN_TUNE_KRYLOV_FUSED      1 (default): each Lanczos step on vectors of at least 2^18
+ *                              entries is one cooperative launch (dot, update, norm, scale
+ *                              with two grid barriers, half the memory traffic); 0: three
+ *                              launches. Runs that share the GPU with concurrent work on
+ *                              other streams set 0.
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,
   PTN_TUNE_ZGEMM_SPLIT_WAVES = 1,
   PTN_TUNE_LARFB_TILE = 2,
   PTN_TUNE_QR_CLUSTER = 3,
-  PTN_TUNE_COUNT = 4
+  PTN_TUNE_KRYLOV_FUSED = 4,
+  PTN_TUNE_COUNT = 5
 };
 ptn_status ptn_tune_set(int key, int value);
 int ptn_tune_get(int key);

@@ -18,6 +18,7 @@ KRYLOV_MAXITER = 64
 PTN_OK, PTN_BAD_SHAPE, PTN_BREAKDOWN, PTN_NAN, PTN_TIMEOUT, PTN_CUDA_ERROR, PTN_UNSUPPORTED = range(7)
 PREC_FP64, PREC_SPLIT_BF16 = 0, 1
 TUNE_TC_SPLIT_WAVES, TUNE_ZGEMM_SPLIT_WAVES, TUNE_LARFB_TILE, TUNE_QR_CLUSTER = 0, 1, 2, 3
+TUNE_KRYLOV_FUSED = 4
 
 
 class PtnError(RuntimeError):

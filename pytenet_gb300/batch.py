@@ -22,6 +22,7 @@ import warnings
 import numpy as np
 import torch
 
+from . import _lib
 from .tdvp import TDVPRun
 
 __all__ = ["BatchTDVP", "tdvp_singlesite_batch", "instance_cost", "assign_streams"]
@@ -88,8 +89,13 @@ class BatchTDVP:
         self.steps_done = 0
 
     def _knobs(self, psi):
-        from .autotune import knobs_for
-        return knobs_for(self.tuning, psi)
+        """The tuned knobs of psi's bucket, and the three-launch Lanczos step: the
+        instances run concurrently on several streams, and the fused step's grid
+        barriers assume the whole GPU."""
+        from .autotune import bucket_values, knobs
+        vals = dict(bucket_values(self.tuning, psi))
+        vals[str(_lib.TUNE_KRYLOV_FUSED)] = 0
+        return knobs(vals)
 
     def _mixed_min_bond(self, psi):
         from .autotune import bucket_values

@@ -39,6 +39,7 @@ struct KState {
   double part_b[RED_MAX];
   int nblocks;                  // CTAs used by the vector passes of this run
   int coef_ready;               // an accepted learned depth already stored coef[]
+  unsigned int bar;             // grid-barrier tickets of the fused Lanczos step
 };
 
 __device__ __forceinline__ double reduce_partials(const double* part, int nb, double* sh) {
@@ -91,6 +92,7 @@ __global__ void __launch_bounds__(VT) k_start_finish(KState* st, const double2* 
       st->s.resid = 0.0;
       st->s.m_target = 0;
       st->coef_ready = 0;
+      st->bar = 0;
       st->nblocks = nb;
     }
   }
@@ -165,6 +167,137 @@ __global__ void __launch_bounds__(VT) k_scale(KState* st, double2* __restrict__ 
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     st->s.beta[j] = beta;
+    st->s.m_used = j + 2;
+  }
+}
+
+// ------------------------------------------------------------------ fused step
+// One Lanczos step (krylov.py:40-51) as one cooperative launch: phase 1 reads w and
+// v_j once into registers (FR entries per thread) and forms the partials of
+// alpha_j = Re <w, v_j>; phase 2, after a grid barrier, forms w - alpha_j v_j -
+// beta_{j-1} v_{j-1} in registers with the partials of |w|^2; phase 3, after a
+// second barrier, tests beta_j against the breakdown threshold and writes
+// v_{j+1} = w / beta_j. Every block reduces the same partials in the same order,
+// so all blocks take identical decisions. Traffic: three vector reads and one
+// write instead of the eight passes of the three-launch step.
+constexpr int FT = 512;           // threads per CTA of the fused step
+constexpr int FR = 4;             // vector entries per thread held in registers
+constexpr long BAR_SPIN_LIMIT = 1L << 24;
+
+// partials written by other CTAs of this grid: read past L1
+__device__ __forceinline__ double reduce_partials_cg(const double* part, int nb, double* sh) {
+  double v = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) v += __ldcg(part + i);
+  return block_sum(v, sh);
+}
+
+// grid-wide barrier over co-resident CTAs (cooperative launch); bounded: on expiry
+// it reports false (the step then stops with PTN_TIMEOUT instead of waiting on)
+__device__ bool grid_barrier(KState* st) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned nb = gridDim.x;
+    const unsigned t = atomicAdd(&st->bar, 1u);
+    const unsigned target = (t / nb + 1u) * nb;
+    int ok = 1;
+    for (long it = 0;; ++it) {
+      unsigned v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(&st->bar) : "memory");
+      if ((int)(v - target) >= 0) break;
+      if (it > BAR_SPIN_LIMIT) {
+        ok = 0;
+        break;
+      }
+      __nanosleep(20);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+__global__ void __launch_bounds__(FT, 2) k_lanczos_fused(KState* st, double2* __restrict__ w,
+                                                         const double2* __restrict__ vj,
+                                                         const double2* __restrict__ vjm1,
+                                                         long n, int j, double thresh) {
+  if (st->s.stopped) return;   // set by earlier launches only: uniform over the grid
+  __shared__ double sh[33];
+  const long T = (long)gridDim.x * FT;
+  const long base = blockIdx.x * (long)FT + threadIdx.x;
+  double2 x[FR], a[FR];
+  double acc = 0.0;
+#pragma unroll
+  for (int r = 0; r < FR; ++r) {
+    const long i = base + r * T;
+    x[r] = make_double2(0.0, 0.0);
+    a[r] = make_double2(0.0, 0.0);
+    if (i < n) {
+      x[r] = w[i];
+      a[r] = vj[i];
+      acc = fma(x[r].x, a[r].x, acc);
+      acc = fma(x[r].y, a[r].y, acc);
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) st->part_a[blockIdx.x] = acc;
+  if (!grid_barrier(st)) {
+    if (threadIdx.x == 0) {
+      st->s.status = PTN_TIMEOUT;
+      st->s.stopped = 1;
+    }
+    return;
+  }
+  const double alpha = reduce_partials_cg(st->part_a, gridDim.x, sh);
+  const double beta = (j > 0) ? st->s.beta[j - 1] : 0.0;
+  acc = 0.0;
+#pragma unroll
+  for (int r = 0; r < FR; ++r) {
+    const long i = base + r * T;
+    if (i < n) {
+      double2 t = make_double2(alpha * a[r].x, alpha * a[r].y);
+      if (j > 0) {
+        const double2 b = vjm1[i];
+        t.x += beta * b.x;
+        t.y += beta * b.y;
+      }
+      x[r].x -= t.x;
+      x[r].y -= t.y;
+      acc = fma(x[r].x, x[r].x, acc);
+      acc = fma(x[r].y, x[r].y, acc);
+    }
+  }
+  acc = block_sum(acc, sh);
+  if (threadIdx.x == 0) st->part_b[blockIdx.x] = acc;
+  if (!grid_barrier(st)) {
+    if (threadIdx.x == 0) {
+      st->s.status = PTN_TIMEOUT;
+      st->s.stopped = 1;
+    }
+    return;
+  }
+  const double bnext = sqrt(reduce_partials_cg(st->part_b, gridDim.x, sh));
+  if (bnext < thresh) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->s.alpha[j] = alpha;
+      st->s.beta_next = bnext;
+      st->s.m_used = j + 1;
+      st->s.stopped = 1;
+      st->s.breakdowns += 1;
+    }
+    return;
+  }
+  const double inv = 1.0 / bnext;
+#pragma unroll
+  for (int r = 0; r < FR; ++r) {
+    const long i = base + r * T;
+    if (i < n) w[i] = make_double2(x[r].x * inv, x[r].y * inv);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    st->s.alpha[j] = alpha;
+    st->s.beta[j] = bnext;
     st->s.m_used = j + 2;
   }
 }
@@ -612,6 +745,34 @@ ptn_status krylov_start(void* state, const double2* vstart, double2* V, long n, 
   return PTN_OK;
 }
 
+// CTAs of the fused Lanczos step for vectors of n entries: all co-resident
+// (cooperative launch), FR entries per thread; 0 when the knob is off or n needs
+// more CTAs than can be resident (the three-launch step is used then)
+int fused_blocks(long n) {
+  // below ~2^18 entries the two grid barriers cost more than the two launches they
+  // replace (measured on GB300 under graph replay: n = 4096: 16.5 us fused, 13.5 us
+  // in three launches; n = 524288: 31.8 us fused, 33.8 us in three launches)
+  constexpr long FUSED_MIN_N = 1L << 18;
+  if (tune(PTN_TUNE_KRYLOV_FUSED) == 0 || n < FUSED_MIN_N) return 0;
+  static int per_sm = -1;
+  if (per_sm < 0) {
+    int v = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, k_lanczos_fused, FT, 0) != cudaSuccess) {
+      cudaGetLastError();
+      v = 0;
+    }
+    per_sm = v;
+  }
+  const long resident = (long)per_sm * num_sms();
+  const long need = (n + (long)FT * FR - 1) / ((long)FT * FR);
+  if (per_sm <= 0 || need > resident || need > RED_MAX) return 0;
+  // about two entries per thread (up to one CTA per SM, for bandwidth), never fewer
+  // CTAs than the registers need, never more than can be resident: small vectors
+  // synchronise few CTAs
+  const long want = std::min<long>((n + 2L * FT - 1) / (2L * FT), std::min<long>(num_sms(), RED_MAX));
+  return (int)std::max<long>(need, want);
+}
+
 ptn_status krylov_step(void* state, double2* V, long n, int j, cudaStream_t st) {
   KState* s = static_cast<KState*>(state);
   const int nb = vec_blocks(n);
@@ -619,6 +780,24 @@ ptn_status krylov_step(void* state, double2* V, long n, int j, cudaStream_t st) 
   double2* w = V + (long)(j + 1) * n;
   const double2* vj = V + (long)j * n;
   const double2* vjm1 = j > 0 ? V + (long)(j - 1) * n : vj;
+  const int fb = fused_blocks(n);
+  if (fb > 0) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(fb);
+    cfg.blockDim = dim3(FT);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const int prof = prof_begin(st, PROF_KRYLOV, 0.0, 64.0 * (double)n);
+    PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_lanczos_fused, s, w, vj, vjm1, n, j, thresh));
+    prof_end(st, prof);
+    note_launches(1);
+    return PTN_OK;
+  }
   k_dot_partial<<<nb, VT, 0, st>>>(s, w, vj, n);
   k_update<<<nb, VT, 0, st>>>(s, w, vj, vjm1, n, j, 1);
   k_scale<<<nb, VT, 0, st>>>(s, w, n, j, thresh);

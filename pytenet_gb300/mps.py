@@ -113,6 +113,19 @@ class MPS:
         dev.download(self)
         return float(nrm.item())
 
+    def compress(self, tol, mode="svd", direction="left"):
+        """Compress and orthonormalise by site-local truncated SVDs on the GPU;
+        returns the original norm and the scaling factor of the compression
+        (pytenet/mps.py:180-236). The reference's "density" mode (rounding by local
+        density matrices, pytenet/mps.py:238-290) is not part of this engine."""
+        if mode == "svd":
+            from .compression import compress_svd
+            return compress_svd(self, tol, direction)
+        if mode == "density":
+            raise NotImplementedError('compress(mode="density") is not provided by pytenet_gb300; '
+                                      'use mode="svd"')
+        raise ValueError(f'`mode` = {mode} invalid; must be "svd" or "density".')
+
     def to_vector(self):
         """Dense vector on the full Hilbert space (pytenet/mps.py:292-301); meant
         for small systems, used as the exact reference in checks."""

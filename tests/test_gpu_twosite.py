@@ -199,3 +199,26 @@ def test_pair_components_match_oracle(ptg):
     xr = orc._site_step(l, r, w2, x, 0.05j, 6)
     print("pair expm", np.abs(to_host(xd) - xr).max() / np.abs(xr).max())
     assert np.abs(to_host(xd) - xr).max() < 1e-11 * np.abs(xr).max()
+
+
+def test_compress_svd_matches_reference(ptg):
+    """MPS.compress(tol, "svd", left / right) on the device (pytenet/mps.py:180-236)
+    against the reference fixture: truncated bond dimensions and quantum numbers
+    bit-exact, norm and compression factor to 1e-12, the compressed state to 1e-10."""
+    g = load_golden("compress.npz")
+    p0 = golden_mps(g, "p0_")
+    for direction in ("left", "right"):
+        psi = ptg.MPS(p0.qsite, p0.qbonds, fill="postpone")
+        psi.a = [x.copy() for x in p0.a]
+        nrm, scale = psi.compress(1e-6, mode="svd", direction=direction)
+        ref = golden_mps(g, f"{direction}_")
+        assert abs(nrm - float(g[f"{direction}_nrm"])) < 1e-12 * abs(float(g[f"{direction}_nrm"]))
+        assert abs(scale - float(g[f"{direction}_scale"])) < 1e-12
+        for qa, qb in zip(psi.qbonds, ref.qbonds):
+            assert np.array_equal(qa, qb)
+        for x, y in zip(psi.a, ref.a):
+            assert x.shape == y.shape
+        v, vr = psi_vector(psi), orc.mps_to_vector(ref)
+        print("compress", direction, "bonds", [len(q) for q in psi.qbonds], "state",
+              np.abs(v - vr).max())
+        assert np.abs(v - vr).max() < 1e-10 * max(1.0, np.abs(vr).max())
