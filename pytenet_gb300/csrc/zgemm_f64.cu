@@ -13,6 +13,13 @@
 // Transposition and conjugation are folded into the global->shared load, so no
 // operand is ever materialised transposed. Skinny problems (fewer tiles than SMs)
 // split K across CTAs and reduce the FP64 partials in a second, deterministic pass.
+//
+// Block sparsity: a K slab whose A part (64 x 16) or B part (16 x 64) of this tile is
+// entirely zero contributes nothing and its DMMAs are skipped (the barrier after the
+// shared-memory store votes on it). Tensors with quantum numbers hold zero blocks
+// (pytenet/block_sparse_util.py:47-64), and after the first block QR every bond is
+// ordered by quantum number, so their blocks line up with tiles and slabs; dense data
+// pays two barrier votes per slab.
 #include "ptn_common.cuh"
 #include <algorithm>
 
@@ -36,6 +43,14 @@ struct OpTraits {
   static constexpr bool trans = (OP == OP_T || OP == OP_H);
   static constexpr bool conj = (OP == OP_C || OP == OP_H);
 };
+
+// whether any of a thread's four loaded entries is non-zero
+__device__ __forceinline__ bool nonzero4(const double2 (&r)[4]) {
+  bool nz = false;
+#pragma unroll
+  for (int i = 0; i < 4; ++i) nz |= (r[i].x != 0.0) | (r[i].y != 0.0);
+  return nz;
+}
 
 // Load op(A)[m0 + m][k0 + k] for the 64x16 tile into registers.
 template <int OA>
@@ -150,11 +165,15 @@ __global__ void __launch_bounds__(THREADS) zgemm_dmma_kernel(const KArgs p) {
     __syncthreads();
     store_a<OA>(ra, sa_re, sa_im);
     store_b<OB>(rb, sb_re, sb_im);
-    __syncthreads();
+    // barrier with a vote: does this slab have a non-zero entry in A's and in B's part
+    const int live_a = __syncthreads_or(nonzero4(ra));
+    const int live_b = __syncthreads_or(nonzero4(rb));
+    const bool live = live_a != 0 && live_b != 0;
     if (k0 + BK < kend) {
       load_a<OA>(ra, A, p.lda, p.M, m0, k0 + BK, kend);
       load_b<OB>(rb, B, p.ldb, p.N, n0, k0 + BK, kend);
     }
+    if (!live) continue;
 #pragma unroll
     for (int kk = 0; kk < BK; kk += 4) {
       double are[4], aim[4], bre[2], bim[2];
