@@ -5,11 +5,11 @@
 // contractions are FP64.
 //
 // Operand conversion ("digits"): a complex matrix view (element (r, k) at
-// src[r * sr + k * sk]) becomes four BF16 digit planes plus one power-of-two
+// src[r * sr + k * sk]) becomes five BF16 digit planes plus one power-of-two
 // exponent per row r. Two tiled passes: the first finds each row's largest
-// |component| (atomicMax of the binary exponent), the second extracts the digits
-// exactly in FP64 arithmetic (scale by 2^(7 - e), then repeated round-to-integer
-// and multiply by 256) and stores them k-contiguously. "Plain" operands keep
+// |component| (atomicMax of the IEEE exponent field), the second forms the
+// fixed-point integer round(x 2^(39 - e)) from the IEEE fields and cuts it into
+// five balanced base-256 digits with integer arithmetic only, stored k-contiguously. "Plain" operands keep
 // re/im interleaved along K; "embedded" operands store z as [[Re, -Im], [Im, Re]].
 //
 // Data flow of H_eff . x (site tensors (Dl, d, Dr), MPO bonds cl / cr):
