@@ -92,8 +92,10 @@ uint64_t ptn_launch_count(void);
  *                              splits than exact integer accumulation needs)
  *   PTN_TUNE_ZGEMM_SPLIT_WAVES split-K target of the FP64 GEMM (0..16, default 2;
  *                              0 = no split-K)
- *   PTN_TUNE_LARFB_TILE        QR block-update tile: 0 chosen per call (default),
- *                              1 16x16, 2 32x16, 3 32x32, 4 64x32 (rows x columns)
+ *   PTN_TUNE_LARFB_TILE        QR block update: 0 register-tiled FMA-only kernels
+ *                              (default); 1..5 the earlier three-pass kernels with
+ *                              tile 1 16x16, 2 32x16, 3 32x32, 4 64x32 (rows x
+ *                              columns) or 5 chosen per call
  *   PTN_TUNE_QR_CLUSTER        largest thread-block cluster of the QR panel: 0 the
  *                              device's (default; at least 32 rows per CTA), or 1..16
  *   PTN_TUNE_KRYLOV_FUSED      1 (default): each Lanczos step on vectors of at least 2^18
@@ -101,6 +103,9 @@ uint64_t ptn_launch_count(void);
  *                              with two grid barriers, half the memory traffic); 0: three
  *                              launches. Runs that share the GPU with concurrent work on
  *                              other streams set 0.
+ *   PTN_TUNE_QR_PANEL          0 (default): QR panel with the reflector scalars and the
+ *                              cluster gather in one warp and the rank-1 updates only
+ *                              on the columns right of the pivot; 1: the earlier panel.
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,
@@ -108,7 +113,8 @@ enum {
   PTN_TUNE_LARFB_TILE = 2,
   PTN_TUNE_QR_CLUSTER = 3,
   PTN_TUNE_KRYLOV_FUSED = 4,
-  PTN_TUNE_COUNT = 5
+  PTN_TUNE_QR_PANEL = 5,
+  PTN_TUNE_COUNT = 6
 };
 ptn_status ptn_tune_set(int key, int value);
 int ptn_tune_get(int key);

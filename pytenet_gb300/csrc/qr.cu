@@ -553,6 +553,203 @@ __global__ void __launch_bounds__(QW * 32) qr_panel4_kernel(double2* __restrict_
   cluster.sync();   // no CTA leaves while its shared memory may still be read
 }
 
+// Panel for GB300's FP64 budget, second form: the same row-per-thread layout and
+// the same two cluster barriers per column as qr_panel4_kernel, with fewer FP64
+// instructions per column on each SM (the FP64 pipe is shared by all of the SM's
+// warps, so work duplicated in every warp is paid once per warp):
+//  - the norm partials of all warps of all CTAs are read directly through DSMEM by
+//    warp 0, which alone forms beta, tau and the scaling (both reciprocals in one
+//    division sequence, on two lanes) and hands them over in shared memory;
+//  - warp 0 alone gathers the reduced vector (all 32 lanes: 16 values x two halves
+//    of the ranks), forms the update scalars conj(tau) w_c (zero for c <= jj) and
+//    keeps the Gram entries;
+//  - the rank-1 update loops only over the columns right of the pivot, reading the
+//    rows from shared memory.
+__global__ void __launch_bounds__(QW * 32) qr_panel5_kernel(double2* __restrict__ a, long lda, int m,
+                                                            int j0, int jb,
+                                                            double2* __restrict__ Tout,
+                                                            double2* __restrict__ V, long ldv) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int cs = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nw = (int)(blockDim.x >> 5);
+  __shared__ double2 xs[NB][QW * 32];     // this CTA's panel rows, column-major
+  __shared__ double s_wn[QW];             // per-warp norm partials (read remotely)
+  __shared__ double2 s_wv[QW][NB];        // per-warp vector partials
+  __shared__ double2 s_alpha;
+  __shared__ double2 s_vec[NB];           // CTA partial vectors (read remotely)
+  __shared__ double2 s_tau[NB];
+  __shared__ double2 s_scal;              // 1 / (alpha - beta)
+  __shared__ double s_beta;
+  __shared__ int s_apply;
+  __shared__ double2 s_upd[NB];           // conj(tau) w_c for c > jj, else 0
+  __shared__ double2 s_G[NB][NB];         // Gram entries v_p^H v_c, p < c (rank 0)
+
+  const int mp = m - j0;
+  const int chunk = (mp + cs - 1) / cs;
+  const int rb = j0 + rank * chunk;
+  const int re = min(m, rb + chunk);
+  const int i = rb + tid;                 // this thread's row
+  const bool mine = i < re;
+
+#pragma unroll
+  for (int c = 0; c < NB; ++c) xs[c][tid] = (mine && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
+  for (int e = tid; e < NB * NB; e += blockDim.x) s_G[e / NB][e % NB] = c2(0.0, 0.0);
+
+#pragma unroll 1
+  for (int jj = 0; jj < jb; ++jj) {
+    const int col = j0 + jj;
+    const int owner = jj / chunk;
+    // ---- norm partials of the part below the diagonal, one per warp
+    const double2 xj = xs[jj][tid];
+    double acc = (mine && i > col) ? fma(xj.x, xj.x, xj.y * xj.y) : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) s_wn[warp] = acc;
+    if (i == col) s_alpha = xj;
+    cluster.sync();
+    // ---- warp 0: the reflector scalars from every warp's partial (fixed order)
+    if (warp == 0) {
+      const int np = cs * nw;              // <= 64
+      double v = 0.0;
+      if (lane < np) v = cluster.map_shared_rank(s_wn, lane / nw)[lane % nw];
+      if (lane + 32 < np) v += cluster.map_shared_rank(s_wn, (lane + 32) / nw)[(lane + 32) % nw];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      const double xn2 = v;
+      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
+      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
+      double beta = 0.0, dx = 0.0, d2 = 1.0;
+      if (apply) {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        dx = alpha.x - beta;
+        d2 = dx * dx + alpha.y * alpha.y;   // |alpha - beta|^2 > 0
+      }
+      // the two reciprocals in one division sequence: lane 0 1 / beta, lane 1 1 / d2
+      const double rec = 1.0 / ((lane == 0) ? (apply ? beta : 1.0) : d2);
+      const double ib = __shfl_sync(0xffffffffu, rec, 0);
+      const double id2 = __shfl_sync(0xffffffffu, rec, 1);
+      if (lane == 0) {
+        double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
+        if (apply) {
+          tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
+          scal = c2(dx * id2, -alpha.y * id2);
+        }
+        s_tau[jj] = tau;
+        s_scal = scal;
+        s_beta = beta;
+        s_apply = apply ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    const bool apply = s_apply != 0;
+    const double2 scal = s_scal;
+    double2 xjn = xj;
+    if (apply && mine && i > col) xjn = cmul(xj, scal);
+    if (apply && i == col) xjn = c2(s_beta, 0.0);
+    xs[jj][tid] = xjn;
+    // ---- one reduction: w_c = v^H a_c (c > jj) and g_p = v_p^H v (p < jj)
+    const double2 vcur = (mine && i >= col) ? ((i == col) ? c2(1.0, 0.0) : xjn) : c2(0.0, 0.0);
+    double2 q[NB];
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      const double2 xc = xs[c][tid];
+      if (c > jj) {
+        q[c] = cmul(cconj(vcur), xc);
+      } else if (c < jj) {
+        const double2 vp = (mine && i >= j0 + c) ? ((i == j0 + c) ? c2(1.0, 0.0) : xc) : c2(0.0, 0.0);
+        q[c] = cmul(cconj(vp), vcur);
+      } else {
+        q[c] = c2(0.0, 0.0);
+      }
+    }
+    const double2 ws = reduce_scatter16(q, lane);
+    const int qi = rs_index(lane);
+    if ((lane & 1) == 0) s_wv[warp][qi] = ws;
+    __syncthreads();
+    if (tid < NB) {
+      const double2 h0 = (nw > 1) ? cadd(s_wv[0][tid], s_wv[1][tid]) : s_wv[0][tid];
+      const double2 h1 = (nw > 2) ? ((nw > 3) ? cadd(s_wv[2][tid], s_wv[3][tid]) : s_wv[2][tid])
+                                  : c2(0.0, 0.0);
+      s_vec[tid] = (nw > 2) ? cadd(h0, h1) : h0;
+    }
+    cluster.sync();
+    // ---- warp 0: lane (c, half) sums the ranks of its half, then the two halves
+    if (warp == 0) {
+      const int c = lane & 15, h = lane >> 4;
+      double2 vals[8];
+#pragma unroll
+      for (int r = 0; r < 8; ++r) {
+        const int rr = h * 8 + r;
+        vals[r] = (rr < cs) ? cluster.map_shared_rank(s_vec, rr)[c] : c2(0.0, 0.0);
+      }
+#pragma unroll
+      for (int hh = 4; hh > 0; hh >>= 1)
+#pragma unroll
+        for (int r = 0; r < hh; ++r) vals[r] = cadd(vals[r], vals[r + hh]);
+      double2 tot = vals[0];
+      tot = cadd(tot, c2(__shfl_xor_sync(0xffffffffu, tot.x, 16),
+                         __shfl_xor_sync(0xffffffffu, tot.y, 16)));
+      if (h == 0) {
+        if (rank == 0 && c < jj) s_G[c][jj] = tot;
+        s_upd[c] = (apply && c > jj) ? cmul(cconj(s_tau[jj]), tot) : c2(0.0, 0.0);
+      }
+    }
+    __syncthreads();
+    // ---- rank-1 update of this thread's row on the columns right of the pivot:
+    // x_c -= v conj(tau) w_c (v = 0 on the rows above the pivot and past the end)
+#pragma unroll 1
+    for (int c = jj + 1; c < jb; ++c) {
+      const double2 s = s_upd[c];
+      double2 x = xs[c][tid];
+      x.x = fma(-vcur.x, s.x, x.x);
+      x.x = fma(vcur.y, s.y, x.x);
+      x.y = fma(-vcur.x, s.y, x.y);
+      x.y = fma(-vcur.y, s.x, x.y);
+      xs[c][tid] = x;
+    }
+  }
+
+  // ---- write the panel back and the explicit V
+  if (mine) {
+#pragma unroll
+    for (int c = 0; c < NB; ++c) {
+      if (c < jb) {
+        const int col = j0 + c;
+        const double2 x = xs[c][tid];
+        a[(long)i * lda + col] = x;
+        V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x;
+      }
+    }
+  }
+  // ---- T (zlarft) on rank 0 from the Gram entries
+  if (rank == 0) {
+    __syncthreads();
+    if (warp == 0) {
+      double2 T[NB];   // lane p holds row p of T
+#pragma unroll
+      for (int c = 0; c < NB; ++c) T[c] = c2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < jb) {
+          double2 acc2 = c2(0.0, 0.0);
+#pragma unroll
+          for (int qq = 0; qq < NB; ++qq)
+            if (qq < c && lane <= qq) acc2 = cfma(T[qq], s_G[qq][c], acc2);
+          const double2 tc = s_tau[c];
+          if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc2);
+          if (lane == c) T[c] = tc;
+        }
+      }
+      if (lane < NB)
+#pragma unroll
+        for (int c = 0; c < NB; ++c) Tout[lane * NB + c] = T[c];
+    }
+  }
+  cluster.sync();   // no CTA leaves while its shared memory may still be read
+}
+
 // partial[rb][j][c] = sum_{rows r of tile rb} conj(V[r][v0 + j]) C[r][c0 + c]
 // lane layout: tr = lane & 7 (row phase), 4 columns per warp, 8 warps -> 32 columns.
 template <int RTT, int CTT>
@@ -671,6 +868,159 @@ __global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__
   }
 }
 
+// ---------------------------------------------------------------------------
+// Register-tiled block reflector application (the default block update):
+//   C <- (I - V op(T) V^H) C   on rows [r0, m), columns [c0, c0 + nc)
+// as three launches
+//   larfb_vhc_kernel   : W_s = V_s^H C_s per (column tile, row split s): one column
+//                        per lane (TC = 32), or per half-warp with two row phases
+//                        (TC = 16, the narrow look-ahead update), the split's rows
+//                        over LW warps, summed over warps and phases in shared memory;
+//   larfb_tw_kernel    : W2 = op(T) sum_s W_s, the splits summed in a fixed order;
+//   larfb_apply_kernel : C -= V W2, one column per lane with its W2 column in registers.
+// On GB300 every FP64 instruction takes a warp slot of the SM's small FP64 pipe, so
+// the inner loops are FMA only (no cross-lane reductions inside the row loop) and
+// the columns past jb are zero rather than predicated off.
+constexpr int LW = 4;   // warps per CTA of the block-update kernels
+
+template <int RPW, int TC>
+__global__ void __launch_bounds__(LW * 32) larfb_vhc_kernel(const double2* __restrict__ C, long ldc,
+                                                            const double2* __restrict__ V, long ldv,
+                                                            int r0, int m, int c0, int nc, int v0,
+                                                            int jb, double2* __restrict__ part) {
+  constexpr int PH = 32 / TC;             // row phases per warp
+  constexpr int RS = LW * RPW * PH;       // rows of one split
+  constexpr int NRED = LW * PH;           // partials per output inside the CTA
+  static_assert(RS * NB <= NRED * NB * TC, "shared buffer sized by the reduction");
+  __shared__ double2 sm[NRED * NB * TC];  // V rows of the split, then the partials
+  const int s = blockIdx.y;
+  const int rbase = r0 + s * RS;
+  for (int idx = threadIdx.x; idx < RS * NB; idx += LW * 32) {
+    const int rr = idx / NB, j = idx % NB;
+    const int r = rbase + rr;
+    sm[idx] = (r < m && j < jb) ? V[(long)r * ldv + v0 + j] : c2(0.0, 0.0);
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int col = lane % TC, ph = lane / TC;
+  const int cl = blockIdx.x * TC + col;
+  const bool live = cl < nc;
+  double2 acc[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) acc[j] = c2(0.0, 0.0);
+  const int rw = warp * RPW * PH + ph;
+#pragma unroll 2
+  for (int i = 0; i < RPW; ++i) {
+    const int rr = rw + i * PH;
+    const int r = rbase + rr;
+    if (r >= m) break;
+    const double2 x = live ? C[(long)r * ldc + c0 + cl] : c2(0.0, 0.0);
+    const double2* vr = sm + rr * NB;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const double2 v = vr[j];
+      acc[j].x = fma(v.x, x.x, acc[j].x);
+      acc[j].x = fma(v.y, x.y, acc[j].x);
+      acc[j].y = fma(v.x, x.y, acc[j].y);
+      acc[j].y = fma(-v.y, x.x, acc[j].y);
+    }
+  }
+  __syncthreads();   // the V rows are no longer needed: reuse the buffer for the partials
+  const int p = warp * PH + ph;
+#pragma unroll
+  for (int j = 0; j < NB; ++j) sm[(p * NB + j) * TC + col] = acc[j];
+  __syncthreads();
+  for (int o = threadIdx.x; o < NB * TC; o += LW * 32) {
+    const int j = o / TC, cc = o % TC;
+    double2 t = sm[o];
+#pragma unroll
+    for (int q = 1; q < NRED; ++q) t = cadd(t, sm[q * NB * TC + o]);
+    const int c = blockIdx.x * TC + cc;
+    if (c < nc) part[((long)s * NB + j) * nc + c] = t;
+  }
+}
+
+// W2 = op(T) sum_s W_s for 16 columns per CTA; W2 replaces split 0 of the partials
+// (every CTA reads and writes only its own columns).
+__global__ void __launch_bounds__(NB * 16) larfb_tw_kernel(double2* __restrict__ part, int nsplit,
+                                                           int nc, int jb,
+                                                           const double2* __restrict__ T,
+                                                           int conjT) {
+  __shared__ double2 sw[NB][16];
+  __shared__ double2 sT[NB][NB];
+  const int j = threadIdx.x / 16, cc = threadIdx.x % 16;
+  const int c = blockIdx.x * 16 + cc;
+  sT[j][cc] = T[j * NB + cc];
+  double2 s0 = c2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
+  if (c < nc && j < jb) {
+    const double2* pp = part + (long)j * nc + c;
+    const long st = (long)NB * nc;
+    int s = 0;
+    for (; s + 4 <= nsplit; s += 4) {
+      s0 = cadd(s0, pp[(long)(s + 0) * st]);
+      s1 = cadd(s1, pp[(long)(s + 1) * st]);
+      s2 = cadd(s2, pp[(long)(s + 2) * st]);
+      s3 = cadd(s3, pp[(long)(s + 3) * st]);
+    }
+    for (; s < nsplit; ++s) s0 = cadd(s0, pp[(long)s * st]);
+  }
+  sw[j][cc] = cadd(cadd(s0, s1), cadd(s2, s3));
+  __syncthreads();
+  double2 w = c2(0.0, 0.0);
+  if (j < jb) {
+    if (conjT) {
+      for (int q = 0; q <= j; ++q) w = cadd(w, cmul(cconj(sT[q][j]), sw[q][cc]));
+    } else {
+      for (int q = j; q < jb; ++q) w = cadd(w, cmul(sT[j][q], sw[q][cc]));
+    }
+  }
+  if (c < nc) part[(long)j * nc + c] = w;
+}
+
+template <int RPW, int TC>
+__global__ void __launch_bounds__(LW * 32) larfb_apply_kernel(double2* __restrict__ C, long ldc,
+                                                              const double2* __restrict__ V, long ldv,
+                                                              int r0, int m, int c0, int nc, int v0,
+                                                              int jb, const double2* __restrict__ W2) {
+  constexpr int PH = 32 / TC;
+  constexpr int RT = LW * RPW * PH;       // rows of one CTA
+  __shared__ double2 sv[RT * NB];
+  const int rbase = r0 + blockIdx.y * RT;
+  for (int idx = threadIdx.x; idx < RT * NB; idx += LW * 32) {
+    const int rr = idx / NB, j = idx % NB;
+    const int r = rbase + rr;
+    sv[idx] = (r < m && j < jb) ? V[(long)r * ldv + v0 + j] : c2(0.0, 0.0);
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int col = lane % TC, ph = lane / TC;
+  const int cl = blockIdx.x * TC + col;
+  const bool live = cl < nc;
+  double2 w[NB];
+#pragma unroll
+  for (int j = 0; j < NB; ++j) w[j] = live ? W2[(long)j * nc + cl] : c2(0.0, 0.0);
+  __syncthreads();
+  if (!live) return;
+  const int rw = warp * RPW * PH + ph;
+#pragma unroll 2
+  for (int i = 0; i < RPW; ++i) {
+    const int rr = rw + i * PH;
+    const int r = rbase + rr;
+    if (r >= m) break;
+    double2* px = C + (long)r * ldc + c0 + cl;
+    double2 x = *px;
+    const double2* vr = sv + rr * NB;
+#pragma unroll
+    for (int j = 0; j < NB; ++j) {
+      const double2 v = vr[j];
+      x.x = fma(-v.x, w[j].x, x.x);
+      x.x = fma(v.y, w[j].y, x.x);
+      x.y = fma(-v.x, w[j].y, x.y);
+      x.y = fma(-v.y, w[j].x, x.y);
+    }
+    *px = x;
+  }
+}
+
 __global__ void extract_r_kernel(const double2* __restrict__ a, long lda, int k, int n,
                                  double2* __restrict__ r, long ldr) {
   const long total = (long)k * n;
@@ -724,11 +1074,56 @@ ptn_status larfb_t(double2* C, long ldc, const double2* V, long ldv, int r0, int
   return PTN_OK;
 }
 
-// the tile shape is chosen per call so that shrinking trailing matrices still
-// launch enough CTAs to keep every SM's FP64 pipes busy
+// register-tiled form: rows per warp chosen so that the launch has about two CTAs
+// per SM (every SM's FP64 pipe busy) while a split keeps at least 16 rows (the
+// workspace holds (m + 15) / 16 splits)
+template <int TC>
+ptn_status larfb_rt(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
+                    int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
+  constexpr int PH = 32 / TC;
+  const long rows = m - r0;
+  const long ctiles = (nc + TC - 1) / TC;
+  const long want = 2L * num_sms();
+  auto splits = [&](int rpw) { return (rows + LW * rpw * PH - 1) / (LW * rpw * PH); };
+  auto choose = [&](int lo) {
+    for (int rpw = 16; rpw > lo; rpw >>= 1)
+      if (ctiles * splits(rpw) >= want) return rpw;
+    return lo;
+  };
+  const int rp = choose(4 / PH);      // partial pass: at least 16 rows per split
+  const int ra = choose(1);           // apply pass
+  const int nsplit = (int)splits(rp);
+  const dim3 gp((unsigned)ctiles, (unsigned)nsplit);
+  switch (rp) {
+    case 16: larfb_vhc_kernel<16, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    case 8: larfb_vhc_kernel<8, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    case 4: larfb_vhc_kernel<4, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    default: larfb_vhc_kernel<2, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+  }
+  larfb_tw_kernel<<<(nc + 15) / 16, NB * 16, 0, st>>>(part, nsplit, nc, jb, T, conjT ? 1 : 0);
+  const dim3 ga((unsigned)ctiles, (unsigned)splits(ra));
+  switch (ra) {
+    case 16: larfb_apply_kernel<16, TC><<<ga, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    case 8: larfb_apply_kernel<8, TC><<<ga, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    case 4: larfb_apply_kernel<4, TC><<<ga, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    case 2: larfb_apply_kernel<2, TC><<<ga, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    default: larfb_apply_kernel<1, TC><<<ga, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+  }
+  PTN_LAUNCH_CHECK();
+  note_launches(3);
+  return PTN_OK;
+}
+
+// PTN_TUNE_LARFB_TILE 0: the register-tiled form (16-column tiles for narrow
+// updates); 1..4 the earlier three-pass kernels with a fixed tile; 5 those kernels
+// with the tile chosen per call so that shrinking trailing matrices still launch
+// enough CTAs to keep every SM's FP64 pipes busy
 ptn_status larfb(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
                  int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
   switch (tune(PTN_TUNE_LARFB_TILE)) {
+    case 0:
+      if (nc <= 16) return larfb_rt<16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
+      return larfb_rt<32>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
     case 1: return larfb_t<16, 16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
     case 2: return larfb_t<32, 16>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
     case 3: return larfb_t<32, 32>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, T, conjT, part, st);
@@ -758,6 +1153,9 @@ int panel_cluster_size() {
                            1) != cudaSuccess)
     cudaGetLastError();
   if (cudaFuncSetAttribute(qr_panel4_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess)
+    cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel5_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
       cudaSuccess)
     cudaGetLastError();
   for (int c : {16, 8}) {
@@ -864,8 +1262,12 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
       attr[0].val.clusterDim.z = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel4_kernel, a, lda, m, j0, jb,
-                                      w.T + (long)p * NB * NB, w.V, (long)k));
+      if (tune(PTN_TUNE_QR_PANEL) == 0)
+        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel5_kernel, a, lda, m, j0, jb,
+                                        w.T + (long)p * NB * NB, w.V, (long)k));
+      else
+        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel4_kernel, a, lda, m, j0, jb,
+                                        w.T + (long)p * NB * NB, w.V, (long)k));
     } else if (cs > 1) {
       cudaLaunchConfig_t cfg = {};
       cfg.gridDim = dim3(cs);

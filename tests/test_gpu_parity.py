@@ -121,6 +121,37 @@ def test_qr_rank_deficient_and_real_input(ptg):
     assert np.allclose(q, qr_, atol=1e-12) and np.allclose(r, rr_, atol=1e-12)
 
 
+@pytest.mark.parametrize("form", [(0, 0), (0, 1), (5, 0), (5, 1)])
+def test_qr_kernel_forms_agree_with_lapack(ptg, form):
+    """Every pairing of the block-update kernels (PTN_TUNE_LARFB_TILE 0: register-
+    tiled, 5: the earlier three-pass form) and of the panel kernels
+    (PTN_TUNE_QR_PANEL 0 / 1) gives numpy.linalg.qr's factors, including on
+    rank-deficient input and on a last panel narrower than 16 columns."""
+    from pytenet_gb300 import _lib
+    L = _lib.load()
+    old = (L.ptn_tune_get(_lib.TUNE_LARFB_TILE), L.ptn_tune_get(_lib.TUNE_QR_PANEL))
+    try:
+        assert L.ptn_tune_set(_lib.TUNE_LARFB_TILE, form[0]) == 0
+        assert L.ptn_tune_set(_lib.TUNE_QR_PANEL, form[1]) == 0
+        rng = np.random.default_rng(77 + form[0] + 10 * form[1])
+        cases = [orc.crandn((1024, 512), rng), orc.crandn((2048, 1000), rng),
+                 orc.crandn((300, 150), rng), orc.crandn((40, 90), rng)]
+        a = orc.crandn((256, 100), rng)
+        a[:, 60:] = 0
+        a[:, 7] = 0
+        a[100:, :] = 0
+        cases.append(a)
+        for a in cases:
+            m, n = a.shape
+            q, r, _ = ptg.block_sparse_qr(a, np.zeros(m, int), np.zeros(n, int))
+            qr_, rr_ = np.linalg.qr(a, mode="reduced")
+            assert np.allclose(q, qr_, rtol=0, atol=1e-11), (m, n)
+            assert np.allclose(r, rr_, rtol=0, atol=1e-11 * max(1, np.abs(rr_).max())), (m, n)
+    finally:
+        L.ptn_tune_set(_lib.TUNE_LARFB_TILE, old[0])
+        L.ptn_tune_set(_lib.TUNE_QR_PANEL, old[1])
+
+
 def test_block_sparse_qr_golden(ptg):
     g = load_golden("block_qr.npz")
     for k in range(int(g["ncases"])):
