@@ -24,6 +24,8 @@ from depth 2 and no network (the baseline the learned depth is measured against)
 Other workloads (one JSON line each, not the headline):
   --workload xxz-d1024     XXZ L=32, D=1024: mixed TDVP against FP64 per step, and DMRG
   --workload ising-batch   256 independent Ising chains (add --autotune)
+  --workload qr            ptn_qr (Q and R) of seeded complex 512x256, 1024x512 and
+                           2048x1024 matrices for each QR kernel form, against LAPACK
 
 Multi-GPU: the sweep does not shard (site i+1 depends on site i), so N GPUs run
 N independent replicas of the workload (weak scaling, no collective on the data
@@ -74,7 +76,7 @@ def parse():
     p.add_argument("--no-graph", dest="graph", action="store_false",
                    help="launch every kernel eagerly instead of replaying each time step as a "
                         "captured CUDA graph")
-    p.add_argument("--workload", default="xxz", choices=["xxz", "ising-batch", "xxz-d1024"])
+    p.add_argument("--workload", default="xxz", choices=["xxz", "ising-batch", "xxz-d1024", "qr"])
     p.add_argument("--dmrg-sweeps", type=int, default=4)
     p.add_argument("--dmrg-acc-sweeps", type=int, default=1)
     p.add_argument("--batch-count", type=int, default=256)
@@ -82,6 +84,8 @@ def parse():
     p.add_argument("--streams", type=int, default=None)
     p.add_argument("--autotune", action="store_true")
     p.add_argument("--cpu-instances", type=int, default=2)
+    p.add_argument("--qr-default-only", action="store_true",
+                   help="--workload qr: only the default kernels on the 1024x512 matrix")
     a = p.parse_args()
     if a.steps is None:
         a.steps = 1 if (a.form == "fp64" or a.workload == "ising-batch") else 5
@@ -851,8 +855,75 @@ def accuracy_vs_fp64(a, ptg, h, psi_host0, qb0, depth_model=None):
     return out, fp64
 
 
+# ------------------------------------------------------------------ QR workload
+
+def qr_arm(a):
+    """ptn_qr with Q formed on the bulk site-tensor shapes (2D x D), one JSON line:
+    median CUDA-event time of 10 calls after 3 warm-up calls, per kernel form
+    (block update PTN_TUNE_LARFB_TILE, panel PTN_TUNE_QR_PANEL), and the largest
+    elementwise difference of Q and R from numpy.linalg.qr."""
+    import torch
+    from pytenet_gb300 import _lib
+    from pytenet_gb300.device import ptr, stream_ptr
+    L = _lib.load()
+    forms = [("earlier three-pass update, one warp per row group", 5, 1),
+             ("register-tiled update, warp-0 scalars and gather", 0, 2),
+             ("register-tiled update, two warps per row group (default)", 0, 0)]
+    shapes = [(512, 256), (1024, 512), (2048, 1024)]
+    if a.qr_default_only:
+        forms, shapes = forms[-1:], [(1024, 512)]
+    old = (L.ptn_tune_get(_lib.TUNE_LARFB_TILE), L.ptn_tune_get(_lib.TUNE_QR_PANEL))
+    res = []
+    try:
+        for (m, n) in shapes:
+            rng = np.random.default_rng(m + n)
+            x = (rng.normal(size=(m, n)) + 1j * rng.normal(size=(m, n))) / np.sqrt(2)
+            q_ref, r_ref = np.linalg.qr(x, mode="reduced")
+            k = min(m, n)
+            dx = torch.from_numpy(x).cuda()
+            work = torch.empty_like(dx)
+            q = torch.empty((m, k), dtype=torch.complex128, device="cuda")
+            r = torch.empty((k, n), dtype=torch.complex128, device="cuda")
+            for what, lt, pn in forms:
+                _lib.check(L.ptn_tune_set(_lib.TUNE_LARFB_TILE, lt))
+                _lib.check(L.ptn_tune_set(_lib.TUNE_QR_PANEL, pn))
+                wsb = L.ptn_qr_workspace_bytes(m, n)
+                ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+                times = []
+                for it in range(13):
+                    work.copy_(dx)
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    e0.record()
+                    _lib.check(L.ptn_qr(ptr(work), m, n, ptr(q), k, ptr(r), n, ptr(ws), wsb,
+                                        stream_ptr()))
+                    e1.record()
+                    torch.cuda.synchronize()
+                    if it >= 3:
+                        times.append(e0.elapsed_time(e1))
+                ms = float(np.median(times))
+                flops = 2 * 8.0 * (m * n * k - (m + n) * k * k / 2.0 + k ** 3 / 3.0)
+                res.append({"m": m, "n": n, "form": what, "larfb_tile": lt, "qr_panel": pn,
+                            "ms": ms, "fp64_tflops": flops / (ms * 1e-3) / 1e12,
+                            "max_err_q": float(np.abs(q.cpu().numpy() - q_ref).max()),
+                            "max_err_r": float(np.abs(r.cpu().numpy() - r_ref).max())})
+    finally:
+        L.ptn_tune_set(_lib.TUNE_LARFB_TILE, old[0])
+        L.ptn_tune_set(_lib.TUNE_QR_PANEL, old[1])
+    best = min(x["ms"] for x in res if (x["m"], x["n"]) == (1024, 512))
+    print(json.dumps({"metric": "ptn_qr time, complex128 1024x512 with Q formed", "value": best,
+                      "unit": "ms", "higher_is_better": False, "dtype": "c128",
+                      "data": "synthetic",
+                      "config": {"workload": "ptn_qr (Q and R) of seeded complex Gaussian "
+                                             "matrices, median of 10 timed calls"},
+                      "forms": res}))
+
+
 def main():
     a = parse()
+    if a.workload == "qr":
+        qr_arm(a)
+        return
     if a.workload == "xxz-d1024":
         precision_arm(a)
         return

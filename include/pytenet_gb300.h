@@ -103,9 +103,11 @@ uint64_t ptn_launch_count(void);
  *                              with two grid barriers, half the memory traffic); 0: three
  *                              launches. Runs that share the GPU with concurrent work on
  *                              other streams set 0.
- *   PTN_TUNE_QR_PANEL          0 (default): QR panel with the reflector scalars and the
- *                              cluster gather in one warp and the rank-1 updates only
- *                              on the columns right of the pivot; 1: the earlier panel.
+ *   PTN_TUNE_QR_PANEL          QR panel kernel: 0 (default) two warps per 32-row group
+ *                              (even / odd columns), one per SM sub-partition for 64-row
+ *                              CTAs; 1 the earlier one-warp-per-row-group panel; 2 that
+ *                              panel with the reflector scalars and the cluster gather
+ *                              in one warp and the updates right of the pivot only.
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,

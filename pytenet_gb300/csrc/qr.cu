@@ -750,6 +750,233 @@ __global__ void __launch_bounds__(QW * 32) qr_panel5_kernel(double2* __restrict_
   cluster.sync();   // no CTA leaves while its shared memory may still be read
 }
 
+// 8 complex values per lane -> lane l holds the warp sum of value rs8_index(l)
+__device__ __forceinline__ double2 reduce_scatter8(double2 (&v)[8], int lane) {
+#pragma unroll
+  for (int lvl = 0, half = 4, mask = 16; lvl < 3; ++lvl, half >>= 1, mask >>= 1) {
+    const bool up = (lane & mask) != 0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      if (i < half) {
+        const double2 send = up ? v[i] : v[i + half];
+        const double2 keep = up ? v[i + half] : v[i];
+        const double2 got = c2(__shfl_xor_sync(0xffffffffu, send.x, mask),
+                               __shfl_xor_sync(0xffffffffu, send.y, mask));
+        v[i] = cadd(keep, got);
+      }
+    }
+  }
+  double2 r = v[0];
+  r = cadd(r, c2(__shfl_xor_sync(0xffffffffu, r.x, 2), __shfl_xor_sync(0xffffffffu, r.y, 2)));
+  return cadd(r, c2(__shfl_xor_sync(0xffffffffu, r.x, 1), __shfl_xor_sync(0xffffffffu, r.y, 1)));
+}
+
+__device__ __forceinline__ int rs8_index(int lane) {
+  return ((lane >> 4) & 1) * 4 + ((lane >> 3) & 1) * 2 + ((lane >> 2) & 1);
+}
+
+// Panel, third form: a 32-row group of the CTA is shared by two warps, one per
+// column set (even / odd columns), so a CTA of 64 rows runs four warps, one on
+// each SM sub-partition, and each warp issues the FP64 work of 8 columns per pivot
+// (dot products, Gram entries, reduction, rank-1 update); interleaving the sets
+// balances the columns right of the pivot between them. Two cluster barriers per
+// column as before; the reflector scalars come from warp 0, the gathered vector
+// from the two warps of row group 0 (one per set).
+constexpr int P6W = 8;   // up to 4 row groups x 2 column sets
+__global__ void __launch_bounds__(P6W * 32) qr_panel6_kernel(double2* __restrict__ a, long lda, int m,
+                                                             int j0, int jb,
+                                                             double2* __restrict__ Tout,
+                                                             double2* __restrict__ V, long ldv) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int cs = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ng = (int)(blockDim.x >> 6);  // row groups
+  const int ch = warp & 1, rg = warp >> 1;
+  __shared__ double2 xs[NB][P6W / 2 * 32];  // this CTA's panel rows, column-major
+  __shared__ double s_wn[P6W / 2];          // norm partials per row group (read remotely)
+  __shared__ double2 s_wv[P6W / 2][NB];     // vector partials per row group
+  __shared__ double2 s_alpha;
+  __shared__ double2 s_vec[NB];             // CTA partial vectors (read remotely)
+  __shared__ double2 s_tau[NB];
+  __shared__ double2 s_scal;
+  __shared__ double s_beta;
+  __shared__ int s_apply;
+  __shared__ double2 s_upd[NB];             // conj(tau) w_c for c > jj, else 0
+  __shared__ double2 s_G[NB][NB];           // Gram entries v_p^H v_c, p < c (rank 0)
+
+  const int mp = m - j0;
+  const int chunk = (mp + cs - 1) / cs;
+  const int rb = j0 + rank * chunk;
+  const int re = min(m, rb + chunk);
+  const int lr = rg * 32 + lane;            // this thread's row within the CTA
+  const int i = rb + lr;
+  const bool mine = i < re;
+
+#pragma unroll
+  for (int t = 0; t < NB / 2; ++t) {
+    const int c = 2 * t + ch;
+    xs[c][lr] = (mine && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
+  }
+  for (int e = tid; e < NB * NB; e += blockDim.x) s_G[e / NB][e % NB] = c2(0.0, 0.0);
+
+#pragma unroll 1
+  for (int jj = 0; jj < jb; ++jj) {
+    const int col = j0 + jj;
+    const int owner = jj / chunk;
+    const int oh = jj & 1;                  // column set holding the pivot
+    // ---- norm partials below the diagonal (the pivot's set), one per row group
+    if (ch == oh) {
+      const double2 xj = xs[jj][lr];
+      double acc = (mine && i > col) ? fma(xj.x, xj.x, xj.y * xj.y) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) s_wn[rg] = acc;
+      if (i == col) s_alpha = xj;
+    }
+    cluster.sync();
+    // ---- warp 0: the reflector scalars from every row group's partial (fixed order)
+    if (warp == 0) {
+      const int np = cs * ng;               // <= 64
+      double v = 0.0;
+      if (lane < np) v = cluster.map_shared_rank(s_wn, lane / ng)[lane % ng];
+      if (lane + 32 < np) v += cluster.map_shared_rank(s_wn, (lane + 32) / ng)[(lane + 32) % ng];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      const double xn2 = v;
+      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
+      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
+      double beta = 0.0, dx = 0.0, d2 = 1.0;
+      if (apply) {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        dx = alpha.x - beta;
+        d2 = dx * dx + alpha.y * alpha.y;
+      }
+      // the two reciprocals in one division sequence: lane 0 1 / beta, lane 1 1 / d2
+      const double rec = 1.0 / ((lane == 0) ? (apply ? beta : 1.0) : d2);
+      const double ib = __shfl_sync(0xffffffffu, rec, 0);
+      const double id2 = __shfl_sync(0xffffffffu, rec, 1);
+      if (lane == 0) {
+        double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
+        if (apply) {
+          tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
+          scal = c2(dx * id2, -alpha.y * id2);
+        }
+        s_tau[jj] = tau;
+        s_scal = scal;
+        s_beta = beta;
+        s_apply = apply ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    const bool apply = s_apply != 0;
+    // the pivot column as updated by the previous pivot (visible after the barriers)
+    const double2 xj = xs[jj][lr];
+    double2 xjn = xj;
+    if (apply && mine && i > col) xjn = cmul(xj, s_scal);
+    if (apply && i == col) xjn = c2(s_beta, 0.0);
+    // ---- one reduction: w_c = v^H a_c (c > jj) and g_p = v_p^H v (p < jj), own set
+    const double2 vcur = (mine && i >= col) ? ((i == col) ? c2(1.0, 0.0) : xjn) : c2(0.0, 0.0);
+    double2 q[NB / 2];
+#pragma unroll
+    for (int t = 0; t < NB / 2; ++t) {
+      const int c = 2 * t + ch;
+      const double2 xc = xs[c][lr];
+      if (c > jj) {
+        q[t] = cmul(cconj(vcur), xc);
+      } else if (c < jj) {
+        const double2 vp = (mine && i >= j0 + c) ? ((i == j0 + c) ? c2(1.0, 0.0) : xc) : c2(0.0, 0.0);
+        q[t] = cmul(cconj(vp), vcur);
+      } else {
+        q[t] = c2(0.0, 0.0);
+      }
+    }
+    const double2 ws = reduce_scatter8(q, lane);
+    if ((lane & 3) == 0) s_wv[rg][2 * rs8_index(lane) + ch] = ws;
+    __syncthreads();
+    if (tid < NB) {
+      double2 s = s_wv[0][tid];
+      if (ng > 1) s = cadd(s, s_wv[1][tid]);
+      if (ng > 2) s = cadd(s, (ng > 3) ? cadd(s_wv[2][tid], s_wv[3][tid]) : s_wv[2][tid]);
+      s_vec[tid] = s;
+    }
+    cluster.sync();
+    // ---- row group 0, one warp per set: lane (t, quarter) sums four ranks, then
+    // the quarters (fixed order, identical in every CTA)
+    if (rg == 0) {
+      const int t = lane & 7, rq = lane >> 3;
+      const int c = 2 * t + ch;
+      double2 vals[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int rr = rq * 4 + k;
+        vals[k] = (rr < cs) ? cluster.map_shared_rank(s_vec, rr)[c] : c2(0.0, 0.0);
+      }
+      double2 tot = cadd(cadd(vals[0], vals[1]), cadd(vals[2], vals[3]));
+      tot = cadd(tot, c2(__shfl_xor_sync(0xffffffffu, tot.x, 8), __shfl_xor_sync(0xffffffffu, tot.y, 8)));
+      tot = cadd(tot, c2(__shfl_xor_sync(0xffffffffu, tot.x, 16), __shfl_xor_sync(0xffffffffu, tot.y, 16)));
+      if (rq == 0) {
+        if (rank == 0 && c < jj) s_G[c][jj] = tot;
+        s_upd[c] = (apply && c > jj) ? cmul(cconj(s_tau[jj]), tot) : c2(0.0, 0.0);
+      }
+    }
+    __syncthreads();
+    // ---- rank-1 update of this thread's row on its set's columns right of the pivot
+#pragma unroll 1
+    for (int t = (jj + 2 - ch) >> 1; 2 * t + ch < jb; ++t) {
+      const int c = 2 * t + ch;
+      const double2 s = s_upd[c];
+      double2 x = xs[c][lr];
+      x.x = fma(-vcur.x, s.x, x.x);
+      x.x = fma(vcur.y, s.y, x.x);
+      x.y = fma(-vcur.x, s.y, x.y);
+      x.y = fma(-vcur.y, s.x, x.y);
+      xs[c][lr] = x;
+    }
+    // the pivot column takes its reflector (every warp has read xj by now)
+    if (ch == oh) xs[jj][lr] = xjn;
+  }
+
+  // ---- write the panel back and the explicit V
+  if (mine) {
+#pragma unroll
+    for (int t = 0; t < NB / 2; ++t) {
+      const int c = 2 * t + ch;
+      if (c < jb) {
+        const int col = j0 + c;
+        const double2 x = xs[c][lr];
+        a[(long)i * lda + col] = x;
+        V[(long)i * ldv + col] = (i < col) ? c2(0.0, 0.0) : (i == col) ? c2(1.0, 0.0) : x;
+      }
+    }
+  }
+  // ---- T (zlarft) on rank 0 from the Gram entries
+  if (rank == 0) {
+    __syncthreads();
+    if (warp == 0) {
+      double2 T[NB];   // lane p holds row p of T
+#pragma unroll
+      for (int c = 0; c < NB; ++c) T[c] = c2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < jb) {
+          double2 acc2 = c2(0.0, 0.0);
+#pragma unroll
+          for (int qq = 0; qq < NB; ++qq)
+            if (qq < c && lane <= qq) acc2 = cfma(T[qq], s_G[qq][c], acc2);
+          const double2 tc = s_tau[c];
+          if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc2);
+          if (lane == c) T[c] = tc;
+        }
+      }
+      if (lane < NB)
+#pragma unroll
+        for (int c = 0; c < NB; ++c) Tout[lane * NB + c] = T[c];
+    }
+  }
+  cluster.sync();   // no CTA leaves while its shared memory may still be read
+}
+
 // partial[rb][j][c] = sum_{rows r of tile rb} conj(V[r][v0 + j]) C[r][c0 + c]
 // lane layout: tr = lane & 7 (row phase), 4 columns per warp, 8 warps -> 32 columns.
 template <int RTT, int CTT>
@@ -876,7 +1103,8 @@ __global__ void __launch_bounds__(256) larfb_update_kernel(double2* __restrict__
 //                        per lane (TC = 32), or per half-warp with two row phases
 //                        (TC = 16, the narrow look-ahead update), the split's rows
 //                        over LW warps, summed over warps and phases in shared memory;
-//   larfb_tw_kernel    : W2 = op(T) sum_s W_s, the splits summed in a fixed order;
+//   larfb_tw1_kernel   : W2 = op(T) sum_s W_s per column, the splits summed in a
+//                        fixed order;
 //   larfb_apply_kernel : C -= V W2, one column per lane with its W2 column in registers.
 // On GB300 every FP64 instruction takes a warp slot of the SM's small FP64 pipe, so
 // the inner loops are FMA only (no cross-lane reductions inside the row loop) and
@@ -940,41 +1168,60 @@ __global__ void __launch_bounds__(LW * 32) larfb_vhc_kernel(const double2* __res
   }
 }
 
-// W2 = op(T) sum_s W_s for 16 columns per CTA; W2 replaces split 0 of the partials
-// (every CTA reads and writes only its own columns).
-__global__ void __launch_bounds__(NB * 16) larfb_tw_kernel(double2* __restrict__ part, int nsplit,
-                                                           int nc, int jb,
-                                                           const double2* __restrict__ T,
-                                                           int conjT) {
-  __shared__ double2 sw[NB][16];
+// W2 = op(T) sum_s W_s, one column per CTA (W2 replaces split 0 of the partials;
+// every CTA reads and writes only its own column). On GB300 each of an SM's four
+// sub-partitions issues one FP64 warp instruction per ~64 cycles, so the split
+// sums and the triangular product are spread over as many SMs as there are
+// columns. Thread
+// (j, part) sums the splits s = part (mod 8) of W[j]; three tree levels combine the
+// parts; thread (j, part) then forms two terms of (op(T) W)[j], combined the same way.
+__global__ void __launch_bounds__(128) larfb_tw1_kernel(double2* __restrict__ part, int nsplit,
+                                                        int nc, int jb,
+                                                        const double2* __restrict__ T,
+                                                        int conjT) {
   __shared__ double2 sT[NB][NB];
-  const int j = threadIdx.x / 16, cc = threadIdx.x % 16;
-  const int c = blockIdx.x * 16 + cc;
-  sT[j][cc] = T[j * NB + cc];
-  double2 s0 = c2(0.0, 0.0), s1 = s0, s2 = s0, s3 = s0;
-  if (c < nc && j < jb) {
-    const double2* pp = part + (long)j * nc + c;
-    const long st = (long)NB * nc;
-    int s = 0;
-    for (; s + 4 <= nsplit; s += 4) {
-      s0 = cadd(s0, pp[(long)(s + 0) * st]);
-      s1 = cadd(s1, pp[(long)(s + 1) * st]);
-      s2 = cadd(s2, pp[(long)(s + 2) * st]);
-      s3 = cadd(s3, pp[(long)(s + 3) * st]);
-    }
-    for (; s < nsplit; ++s) s0 = cadd(s0, pp[(long)s * st]);
-  }
-  sw[j][cc] = cadd(cadd(s0, s1), cadd(s2, s3));
-  __syncthreads();
-  double2 w = c2(0.0, 0.0);
+  __shared__ double2 sp[8][NB];
+  __shared__ double2 sw[NB];
+  const int c = blockIdx.x;
+  const int j = threadIdx.x & 15, pp = threadIdx.x >> 4;
+  for (int e = threadIdx.x; e < NB * NB; e += 128) sT[e / NB][e % NB] = T[e];
+  double2 s0 = c2(0.0, 0.0), s1 = s0;
   if (j < jb) {
-    if (conjT) {
-      for (int q = 0; q <= j; ++q) w = cadd(w, cmul(cconj(sT[q][j]), sw[q][cc]));
-    } else {
-      for (int q = j; q < jb; ++q) w = cadd(w, cmul(sT[j][q], sw[q][cc]));
+    const double2* src = part + (long)j * nc + c;
+    const long st = (long)NB * nc;
+    int s = pp;
+    for (; s + 8 < nsplit; s += 16) {
+      s0 = cadd(s0, src[(long)s * st]);
+      s1 = cadd(s1, src[(long)(s + 8) * st]);
+    }
+    if (s < nsplit) s0 = cadd(s0, src[(long)s * st]);
+  }
+  sp[pp][j] = cadd(s0, s1);
+  __syncthreads();
+  if (pp < 4) sp[pp][j] = cadd(sp[pp][j], sp[pp + 4][j]);
+  __syncthreads();
+  if (pp < 2) sp[pp][j] = cadd(sp[pp][j], sp[pp + 2][j]);
+  __syncthreads();
+  if (pp == 0) sw[j] = cadd(sp[0][j], sp[1][j]);
+  __syncthreads();
+  // (op(T) W)[j] = sum_q op(T)[j][q] W[q]; thread (j, pp) takes q = pp and pp + 8
+  double2 acc = c2(0.0, 0.0);
+  if (j < jb) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int q = pp + 8 * h;
+      const double2 t = conjT ? cconj(sT[q][j]) : sT[j][q];
+      const bool tri = conjT ? (q <= j) : (q >= j && q < jb);
+      if (tri) acc = cfma(t, sw[q], acc);
     }
   }
-  if (c < nc) part[(long)j * nc + c] = w;
+  sp[pp][j] = acc;
+  __syncthreads();
+  if (pp < 4) sp[pp][j] = cadd(sp[pp][j], sp[pp + 4][j]);
+  __syncthreads();
+  if (pp < 2) sp[pp][j] = cadd(sp[pp][j], sp[pp + 2][j]);
+  __syncthreads();
+  if (pp == 0) part[(long)j * nc + c] = cadd(sp[0][j], sp[1][j]);
 }
 
 template <int RPW, int TC>
@@ -1075,8 +1322,8 @@ ptn_status larfb_t(double2* C, long ldc, const double2* V, long ldv, int r0, int
 }
 
 // register-tiled form: rows per warp chosen so that the launch has about two CTAs
-// per SM (every SM's FP64 pipe busy) while a split keeps at least 16 rows (the
-// workspace holds (m + 15) / 16 splits)
+// per SM (every SM's FP64 pipe busy) while a split keeps at least 8 rows (the
+// workspace holds (m + 7) / 8 splits)
 template <int TC>
 ptn_status larfb_rt(double2* C, long ldc, const double2* V, long ldv, int r0, int m, int c0, int nc,
                     int v0, int jb, const double2* T, bool conjT, double2* part, cudaStream_t st) {
@@ -1090,7 +1337,7 @@ ptn_status larfb_rt(double2* C, long ldc, const double2* V, long ldv, int r0, in
       if (ctiles * splits(rpw) >= want) return rpw;
     return lo;
   };
-  const int rp = choose(4 / PH);      // partial pass: at least 16 rows per split
+  const int rp = choose(2 / PH);      // partial pass: at least 8 rows per split
   const int ra = choose(1);           // apply pass
   const int nsplit = (int)splits(rp);
   const dim3 gp((unsigned)ctiles, (unsigned)nsplit);
@@ -1098,9 +1345,10 @@ ptn_status larfb_rt(double2* C, long ldc, const double2* V, long ldv, int r0, in
     case 16: larfb_vhc_kernel<16, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
     case 8: larfb_vhc_kernel<8, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
     case 4: larfb_vhc_kernel<4, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
-    default: larfb_vhc_kernel<2, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    case 2: larfb_vhc_kernel<2, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
+    default: larfb_vhc_kernel<1, TC><<<gp, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
   }
-  larfb_tw_kernel<<<(nc + 15) / 16, NB * 16, 0, st>>>(part, nsplit, nc, jb, T, conjT ? 1 : 0);
+  larfb_tw1_kernel<<<nc, 128, 0, st>>>(part, nsplit, nc, jb, T, conjT ? 1 : 0);
   const dim3 ga((unsigned)ctiles, (unsigned)splits(ra));
   switch (ra) {
     case 16: larfb_apply_kernel<16, TC><<<ga, LW * 32, 0, st>>>(C, ldc, V, ldv, r0, m, c0, nc, v0, jb, part); break;
@@ -1156,6 +1404,9 @@ int panel_cluster_size() {
       cudaSuccess)
     cudaGetLastError();
   if (cudaFuncSetAttribute(qr_panel5_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess)
+    cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel6_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
       cudaSuccess)
     cudaGetLastError();
   for (int c : {16, 8}) {
@@ -1223,7 +1474,7 @@ int side_index(cudaStream_t st) {
 size_t qr_workspace_bytes(int m, int n) {
   const int k = std::min(m, n);
   const int np = (k + NB - 1) / NB;
-  const int nrb = (m + 15) / 16;   // smallest row tile of the block update
+  const int nrb = (m + 7) / 8;     // most row splits of a block update
   return al((size_t)m * k * sizeof(double2)) + al((size_t)np * NB * NB * sizeof(double2)) +
          al((size_t)nrb * NB * std::max(n, k) * sizeof(double2));
 }
@@ -1251,8 +1502,10 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
     const int chunk = cs > 1 ? (m - j0 + cs - 1) / cs : m - j0;
     if (chunk <= QW * 32) {   // a cluster of one CTA is the single-CTA case
       cudaLaunchConfig_t cfg = {};
+      const int form = tune(PTN_TUNE_QR_PANEL);
       cfg.gridDim = dim3(cs);
-      cfg.blockDim = dim3(32 * ((chunk + 31) / 32));   // warps the row chunk needs
+      // warps the row chunk needs (two per 32-row group for the default panel)
+      cfg.blockDim = dim3((form == 0 ? 64 : 32) * ((chunk + 31) / 32));
       cfg.dynamicSmemBytes = 0;
       cfg.stream = st;
       cudaLaunchAttribute attr[1];
@@ -1262,7 +1515,10 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
       attr[0].val.clusterDim.z = 1;
       cfg.attrs = attr;
       cfg.numAttrs = 1;
-      if (tune(PTN_TUNE_QR_PANEL) == 0)
+      if (form == 0)
+        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel6_kernel, a, lda, m, j0, jb,
+                                        w.T + (long)p * NB * NB, w.V, (long)k));
+      else if (form == 2)
         PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel5_kernel, a, lda, m, j0, jb,
                                         w.T + (long)p * NB * NB, w.V, (long)k));
       else
