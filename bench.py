@@ -868,7 +868,8 @@ def qr_arm(a):
     L = _lib.load()
     forms = [("earlier three-pass update, one warp per row group", 5, 1),
              ("register-tiled update, warp-0 scalars and gather", 0, 2),
-             ("register-tiled update, two warps per row group (default)", 0, 0)]
+             ("register-tiled update, two warps per row group, reduce-scatter", 0, 3),
+             ("register-tiled update, two warps per row group, shared-memory sums (default)", 0, 0)]
     shapes = [(512, 256), (1024, 512), (2048, 1024)]
     if a.qr_default_only:
         forms, shapes = forms[-1:], [(1024, 512)]

@@ -104,10 +104,12 @@ uint64_t ptn_launch_count(void);
  *                              launches. Runs that share the GPU with concurrent work on
  *                              other streams set 0.
  *   PTN_TUNE_QR_PANEL          QR panel kernel: 0 (default) two warps per 32-row group
- *                              (even / odd columns), one per SM sub-partition for 64-row
- *                              CTAs; 1 the earlier one-warp-per-row-group panel; 2 that
- *                              panel with the reflector scalars and the cluster gather
- *                              in one warp and the updates right of the pivot only.
+ *                              (even / odd columns, one per SM sub-partition for 64-row
+ *                              CTAs), select-free products summed through shared memory,
+ *                              next pivot's norm published before the other updates;
+ *                              3 the same layout with a shuffle reduce-scatter; 1 the
+ *                              earlier one-warp-per-row-group panel; 2 that panel with
+ *                              the reflector scalars and the cluster gather in one warp.
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,

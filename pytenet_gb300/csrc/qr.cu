@@ -977,6 +977,231 @@ __global__ void __launch_bounds__(P6W * 32) qr_panel6_kernel(double2* __restrict
   cluster.sync();   // no CTA leaves while its shared memory may still be read
 }
 
+__device__ __forceinline__ void cluster_arrive() {
+  asm volatile("barrier.cluster.arrive.release;" ::: "memory");
+}
+__device__ __forceinline__ void cluster_wait() {
+  asm volatile("barrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// Panel, fourth form (default): the layout of qr_panel6_kernel (two warps per 32-row
+// group, even / odd columns) with a shorter instruction path per column:
+//  - one product per row and column, conj(v) x_c, for every column: on the rows
+//    where a masked operand would differ, v is zero, so the dot products (c > jj)
+//    and the conjugated Gram entries (c < jj) come out of the same select-free loop;
+//  - the products go to shared memory (rows x 17 complex, conflict-free) and
+//    thread (column, 8-row block) sums them: one pass instead of a shuffle
+//    reduce-scatter with selects;
+//  - after the gather, the next pivot column is updated first and its norm partial
+//    published; the cluster barrier that guards it is split (arrive now, wait at the
+//    next pivot), so the other updates run while the barrier completes.
+// Dynamic shared memory: xs[NB][R] and the product buffer [R][17], R = 32 x row groups.
+__global__ void __launch_bounds__(P6W * 32) qr_panel7_kernel(double2* __restrict__ a, long lda, int m,
+                                                             int j0, int jb,
+                                                             double2* __restrict__ Tout,
+                                                             double2* __restrict__ V, long ldv) {
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = (int)cluster.block_rank();
+  const int cs = (int)cluster.num_blocks();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int ng = (int)(blockDim.x >> 6);   // row groups
+  const int nw = 2 * ng;
+  const int R = 32 * ng;                   // rows held by this CTA
+  const int ch = warp & 1, rg = warp >> 1;
+  extern __shared__ double2 dyn[];
+  double2* xs = dyn;                       // xs[c * R + row]
+  double2* qs = dyn + NB * R;              // qs[row * 17 + c]
+  __shared__ double s_wn[P6W / 2];
+  __shared__ double2 s_wv[P6W][NB];        // per-warp column sums
+  __shared__ double2 s_alpha;
+  __shared__ double2 s_vec[NB];            // CTA column sums (read remotely)
+  __shared__ double2 s_tau[NB];
+  __shared__ double2 s_scal;
+  __shared__ double s_beta;
+  __shared__ int s_apply;
+  __shared__ double2 s_upd[NB];
+  __shared__ double2 s_G[NB][NB];
+
+  const int mp = m - j0;
+  const int chunk = (mp + cs - 1) / cs;
+  const int rb = j0 + rank * chunk;
+  const int re = min(m, rb + chunk);
+  const int lr = rg * 32 + lane;
+  const int i = rb + lr;
+  const bool mine = i < re;
+
+#pragma unroll
+  for (int t = 0; t < NB / 2; ++t) {
+    const int c = 2 * t + ch;
+    xs[c * R + lr] = (mine && c < jb) ? a[(long)i * lda + j0 + c] : c2(0.0, 0.0);
+  }
+  for (int e = tid; e < NB * NB; e += blockDim.x) s_G[e / NB][e % NB] = c2(0.0, 0.0);
+
+  // norm partial of pivot column p (its set's warps) and the pivot entry
+  auto publish_norm = [&](int p) {
+    if (ch == (p & 1)) {
+      const double2 x = xs[p * R + lr];
+      double acc = (mine && i > j0 + p) ? fma(x.x, x.x, x.y * x.y) : 0.0;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+      if (lane == 0) s_wn[rg] = acc;
+      if (i == j0 + p) s_alpha = x;
+    }
+  };
+  publish_norm(0);
+  cluster_arrive();
+
+#pragma unroll 1
+  for (int jj = 0; jj < jb; ++jj) {
+    const int col = j0 + jj;
+    const int owner = jj / chunk;
+    const int oh = jj & 1;
+    cluster_wait();
+    // ---- warp 0: the reflector scalars (fixed summation order)
+    if (warp == 0) {
+      const int np = cs * ng;
+      double v = 0.0;
+      if (lane < np) v = cluster.map_shared_rank(s_wn, lane / ng)[lane % ng];
+      if (lane + 32 < np) v += cluster.map_shared_rank(s_wn, (lane + 32) / ng)[(lane + 32) % ng];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      const double xn2 = v;
+      const double2 alpha = *cluster.map_shared_rank(&s_alpha, owner);
+      const bool apply = !(xn2 == 0.0 && alpha.y == 0.0);
+      double beta = 0.0, dx = 0.0, d2 = 1.0;
+      if (apply) {
+        beta = -copysign(sqrt(alpha.x * alpha.x + alpha.y * alpha.y + xn2), alpha.x);
+        dx = alpha.x - beta;
+        d2 = dx * dx + alpha.y * alpha.y;
+      }
+      const double rec = 1.0 / ((lane == 0) ? (apply ? beta : 1.0) : d2);
+      const double ib = __shfl_sync(0xffffffffu, rec, 0);
+      const double id2 = __shfl_sync(0xffffffffu, rec, 1);
+      if (lane == 0) {
+        double2 tau = c2(0.0, 0.0), scal = c2(0.0, 0.0);
+        if (apply) {
+          tau = c2((beta - alpha.x) * ib, -alpha.y * ib);
+          scal = c2(dx * id2, -alpha.y * id2);
+        }
+        s_tau[jj] = tau;
+        s_scal = scal;
+        s_beta = beta;
+        s_apply = apply ? 1 : 0;
+      }
+    }
+    __syncthreads();
+    const bool apply = s_apply != 0;
+    const double2 xj = xs[jj * R + lr];
+    double2 xjn = xj;
+    if (apply && mine && i > col) xjn = cmul(xj, s_scal);
+    if (apply && i == col) xjn = c2(s_beta, 0.0);
+    const double2 vcur = (mine && i >= col) ? ((i == col) ? c2(1.0, 0.0) : xjn) : c2(0.0, 0.0);
+    const double2 vc = cconj(vcur);
+    // ---- products conj(v) x_c of this row, own set
+#pragma unroll
+    for (int t = 0; t < NB / 2; ++t) {
+      const int c = 2 * t + ch;
+      qs[lr * 17 + c] = cmul(vc, xs[c * R + lr]);
+    }
+    __syncthreads();
+    // ---- column sums: thread (c, 8-row block), the two blocks of a warp, per warp
+    {
+      const int c = tid & 15, p = tid >> 4;
+      const double2* src = qs + (8 * p) * 17 + c;
+      double2 s01 = cadd(src[0 * 17], src[1 * 17]), s23 = cadd(src[2 * 17], src[3 * 17]);
+      double2 s45 = cadd(src[4 * 17], src[5 * 17]), s67 = cadd(src[6 * 17], src[7 * 17]);
+      double2 s = cadd(cadd(s01, s23), cadd(s45, s67));
+      s = cadd(s, c2(__shfl_xor_sync(0xffffffffu, s.x, 16), __shfl_xor_sync(0xffffffffu, s.y, 16)));
+      if (lane < 16) s_wv[warp][c] = s;
+    }
+    __syncthreads();
+    if (tid < NB) {
+      double2 s = s_wv[0][tid];
+      for (int w = 1; w < nw; ++w) s = cadd(s, s_wv[w][tid]);
+      s_vec[tid] = s;
+    }
+    cluster.sync();
+    // ---- row group 0, one warp per set: gather four ranks per lane, then the quarters
+    if (rg == 0) {
+      const int t = lane & 7, rq = lane >> 3;
+      const int c = 2 * t + ch;
+      double2 vals[4];
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int rr = rq * 4 + k;
+        vals[k] = (rr < cs) ? cluster.map_shared_rank(s_vec, rr)[c] : c2(0.0, 0.0);
+      }
+      double2 tot = cadd(cadd(vals[0], vals[1]), cadd(vals[2], vals[3]));
+      tot = cadd(tot, c2(__shfl_xor_sync(0xffffffffu, tot.x, 8), __shfl_xor_sync(0xffffffffu, tot.y, 8)));
+      tot = cadd(tot, c2(__shfl_xor_sync(0xffffffffu, tot.x, 16), __shfl_xor_sync(0xffffffffu, tot.y, 16)));
+      if (rq == 0) {
+        if (rank == 0 && c < jj) s_G[c][jj] = cconj(tot);   // v_c^H v_jj
+        s_upd[c] = (apply && c > jj) ? cmul(cconj(s_tau[jj]), tot) : c2(0.0, 0.0);
+      }
+    }
+    __syncthreads();
+    // ---- next pivot first: update, publish its norm, arrive; then the rest
+    auto upd = [&](int c) {
+      const double2 s = s_upd[c];
+      double2 x = xs[c * R + lr];
+      x.x = fma(-vcur.x, s.x, x.x);
+      x.x = fma(vcur.y, s.y, x.x);
+      x.y = fma(-vcur.x, s.y, x.y);
+      x.y = fma(-vcur.y, s.x, x.y);
+      xs[c * R + lr] = x;
+    };
+    if (ch == oh) xs[jj * R + lr] = xjn;   // the pivot column takes its reflector
+    if (jj + 1 < jb) {
+      if (ch != oh) upd(jj + 1);
+      publish_norm(jj + 1);
+      cluster_arrive();
+    }
+#pragma unroll 1
+    for (int t = (jj + 3 - ch) >> 1; 2 * t + ch < jb; ++t) upd(2 * t + ch);
+  }
+
+  // ---- write the panel back and the explicit V
+  if (mine) {
+#pragma unroll
+    for (int t = 0; t < NB / 2; ++t) {
+      const int c = 2 * t + ch;
+      if (c < jb) {
+        const int colc = j0 + c;
+        const double2 x = xs[c * R + lr];
+        a[(long)i * lda + colc] = x;
+        V[(long)i * ldv + colc] = (i < colc) ? c2(0.0, 0.0) : (i == colc) ? c2(1.0, 0.0) : x;
+      }
+    }
+  }
+  // ---- T (zlarft) on rank 0 from the Gram entries
+  if (rank == 0) {
+    __syncthreads();
+    if (warp == 0) {
+      double2 T[NB];
+#pragma unroll
+      for (int c = 0; c < NB; ++c) T[c] = c2(0.0, 0.0);
+#pragma unroll
+      for (int c = 0; c < NB; ++c) {
+        if (c < jb) {
+          double2 acc2 = c2(0.0, 0.0);
+#pragma unroll
+          for (int qq = 0; qq < NB; ++qq)
+            if (qq < c && lane <= qq) acc2 = cfma(T[qq], s_G[qq][c], acc2);
+          const double2 tc = s_tau[c];
+          if (lane < c) T[c] = cmul(c2(-tc.x, -tc.y), acc2);
+          if (lane == c) T[c] = tc;
+        }
+      }
+      if (lane < NB)
+#pragma unroll
+        for (int c = 0; c < NB; ++c) Tout[lane * NB + c] = T[c];
+    }
+  }
+  cluster.sync();   // no CTA leaves while its shared memory may still be read
+}
+
+size_t panel7_smem_bytes(int ng) { return (size_t)(NB * 32 * ng + 32 * ng * 17) * sizeof(double2); }
+
 // partial[rb][j][c] = sum_{rows r of tile rb} conj(V[r][v0 + j]) C[r][c0 + c]
 // lane layout: tr = lane & 7 (row phase), 4 columns per warp, 8 warps -> 32 columns.
 template <int RTT, int CTT>
@@ -1185,18 +1410,23 @@ __global__ void __launch_bounds__(128) larfb_tw1_kernel(double2* __restrict__ pa
   const int c = blockIdx.x;
   const int j = threadIdx.x & 15, pp = threadIdx.x >> 4;
   for (int e = threadIdx.x; e < NB * NB; e += 128) sT[e / NB][e % NB] = T[e];
-  double2 s0 = c2(0.0, 0.0), s1 = s0;
+  double2 s0 = c2(0.0, 0.0);
   if (j < jb) {
     const double2* src = part + (long)j * nc + c;
     const long st = (long)NB * nc;
-    int s = pp;
-    for (; s + 8 < nsplit; s += 16) {
-      s0 = cadd(s0, src[(long)s * st]);
-      s1 = cadd(s1, src[(long)(s + 8) * st]);
+    // eight independent loads in flight per round, summed as a tree
+    for (int base = pp; base < nsplit; base += 64) {
+      double2 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int s = base + 8 * u;
+        v[u] = (s < nsplit) ? src[(long)s * st] : c2(0.0, 0.0);
+      }
+      s0 = cadd(s0, cadd(cadd(cadd(v[0], v[1]), cadd(v[2], v[3])),
+                         cadd(cadd(v[4], v[5]), cadd(v[6], v[7]))));
     }
-    if (s < nsplit) s0 = cadd(s0, src[(long)s * st]);
   }
-  sp[pp][j] = cadd(s0, s1);
+  sp[pp][j] = s0;
   __syncthreads();
   if (pp < 4) sp[pp][j] = cadd(sp[pp][j], sp[pp + 4][j]);
   __syncthreads();
@@ -1409,6 +1639,12 @@ int panel_cluster_size() {
   if (cudaFuncSetAttribute(qr_panel6_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
       cudaSuccess)
     cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel7_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess)
+    cudaGetLastError();
+  if (cudaFuncSetAttribute(qr_panel7_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)panel7_smem_bytes(P6W / 2)) != cudaSuccess)
+    cudaGetLastError();
   for (int c : {16, 8}) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(c);
@@ -1503,10 +1739,11 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
     if (chunk <= QW * 32) {   // a cluster of one CTA is the single-CTA case
       cudaLaunchConfig_t cfg = {};
       const int form = tune(PTN_TUNE_QR_PANEL);
+      const int ngroups = (chunk + 31) / 32;
       cfg.gridDim = dim3(cs);
-      // warps the row chunk needs (two per 32-row group for the default panel)
-      cfg.blockDim = dim3((form == 0 ? 64 : 32) * ((chunk + 31) / 32));
-      cfg.dynamicSmemBytes = 0;
+      // warps the row chunk needs (two per 32-row group for the two-set panels)
+      cfg.blockDim = dim3((form == 0 || form == 3 ? 64 : 32) * ngroups);
+      cfg.dynamicSmemBytes = form == 0 ? panel7_smem_bytes(ngroups) : 0;
       cfg.stream = st;
       cudaLaunchAttribute attr[1];
       attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -1516,6 +1753,9 @@ ptn_status qr(double2* a, int m, int n, double2* q, long ldq, double2* r, long l
       cfg.attrs = attr;
       cfg.numAttrs = 1;
       if (form == 0)
+        PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel7_kernel, a, lda, m, j0, jb,
+                                        w.T + (long)p * NB * NB, w.V, (long)k));
+      else if (form == 3)
         PTN_CUDA_TRY(cudaLaunchKernelEx(&cfg, qr_panel6_kernel, a, lda, m, j0, jb,
                                         w.T + (long)p * NB * NB, w.V, (long)k));
       else if (form == 2)

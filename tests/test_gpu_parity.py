@@ -121,11 +121,11 @@ def test_qr_rank_deficient_and_real_input(ptg):
     assert np.allclose(q, qr_, atol=1e-12) and np.allclose(r, rr_, atol=1e-12)
 
 
-@pytest.mark.parametrize("form", [(0, 0), (0, 1), (0, 2), (5, 0), (5, 1)])
+@pytest.mark.parametrize("form", [(0, 0), (0, 1), (0, 2), (0, 3), (5, 0), (5, 1)])
 def test_qr_kernel_forms_agree_with_lapack(ptg, form):
     """Every pairing of the block-update kernels (PTN_TUNE_LARFB_TILE 0: register-
     tiled, 5: the earlier three-pass form) and of the panel kernels
-    (PTN_TUNE_QR_PANEL 0 / 1 / 2) gives numpy.linalg.qr's factors, including on
+    (PTN_TUNE_QR_PANEL 0 .. 3) gives numpy.linalg.qr's factors, including on
     rank-deficient input and on a last panel narrower than 16 columns."""
     from pytenet_gb300 import _lib
     L = _lib.load()
