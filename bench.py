@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--depth-tol", type=float, default=1e-10)
     p.add_argument("--tc-split-waves", type=int, default=None,
                    help="PTN_TUNE_TC_SPLIT_WAVES for the run (library default if unset)")
+    p.add_argument("--tc-persistent", type=int, default=None, choices=[0, 1],
+                   help="PTN_TUNE_TC_PERSISTENT for the run (library default if unset)")
     p.add_argument("--L", type=int, default=64)
     p.add_argument("--D", type=int, default=512)
     p.add_argument("--m", type=int, default=10)
@@ -337,6 +339,8 @@ def our_arm(a):
 
     if a.tc_split_waves is not None:
         _lib.check(L.ptn_tune_set(_lib.TUNE_TC_SPLIT_WAVES, a.tc_split_waves))
+    if a.tc_persistent is not None:
+        _lib.check(L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, a.tc_persistent))
     h, psi, delta = make_workload(a, ptg)
     psi.orthonormalize(mode="left")
     psi_host0 = [x.copy() for x in psi.a]
@@ -494,6 +498,7 @@ def our_arm(a):
                "config": {"workload": workload_desc(a), "form": a.form, "L": a.L, "D": a.D,
                           "numiter_lanczos": a.m, "delta": delta, "graph": a.graph,
                           "tc_split_waves": L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES),
+                          "tc_persistent": L.ptn_tune_get(_lib.TUNE_TC_PERSISTENT),
                           "parallelism": f"replicas x{world}",
                           "l2": "inputs larger than L2 (state of several GB per replica)"},
                "krylov": krylov, "clocks": clk, "e2e": e2e, "gpu_launches": int(launches), "roofline": roofline,

@@ -110,6 +110,9 @@ uint64_t ptn_launch_count(void);
  *                              3 the same layout with a shuffle reduce-scatter; 1 the
  *                              earlier one-warp-per-row-group panel; 2 that panel with
  *                              the reflector scalars and the cluster gather in one warp.
+ *   PTN_TUNE_TC_PERSISTENT     1 (default): the tensor-core GEMM runs one CTA per SM over
+ *                              all (tile, K split) units, the next unit's loads and MMAs
+ *                              overlapping the current one's epilogue; 0: one CTA per unit.
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,
@@ -118,7 +121,8 @@ enum {
   PTN_TUNE_QR_CLUSTER = 3,
   PTN_TUNE_KRYLOV_FUSED = 4,
   PTN_TUNE_QR_PANEL = 5,
-  PTN_TUNE_COUNT = 6
+  PTN_TUNE_TC_PERSISTENT = 6,
+  PTN_TUNE_COUNT = 7
 };
 ptn_status ptn_tune_set(int key, int value);
 int ptn_tune_get(int key);

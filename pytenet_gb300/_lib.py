@@ -20,6 +20,7 @@ PREC_FP64, PREC_SPLIT_BF16 = 0, 1
 TUNE_TC_SPLIT_WAVES, TUNE_ZGEMM_SPLIT_WAVES, TUNE_LARFB_TILE, TUNE_QR_CLUSTER = 0, 1, 2, 3
 TUNE_KRYLOV_FUSED = 4
 TUNE_QR_PANEL = 5
+TUNE_TC_PERSISTENT = 6
 
 
 class PtnError(RuntimeError):

@@ -491,6 +491,274 @@ __global__ void __launch_bounds__(THREADS, 1)
   }
 }
 
+// Persistent form of tc_gemm_kernel: one CTA per SM walks the work units
+// u = blockIdx.x, blockIdx.x + gridDim.x, ... (u -> N tile fastest, then M tile,
+// then K split), with the same warp roles, the same digit pairs and the same exact
+// periods per unit. The stage ring, the period count of tfull / tempty and the
+// unit count of tdone / tfree continue from unit to unit, so the TMA producer
+// fetches the next unit's first K blocks while the current one is finished, and
+// the MMA warp starts the next unit as soon as the epilogue has read the last
+// accumulator columns out of tensor memory (tfree); the epilogue converts into its
+// registers first and writes the outputs while the next unit's MMAs run. TMEM is
+// allocated and the barriers initialised once per CTA.
+__global__ void __launch_bounds__(THREADS, 1)
+    tc_gemm_persistent_kernel(const __grid_constant__ CUtensorMap tmA,
+                              const __grid_constant__ CUtensorMap tmB, const TcArgs p, int gx,
+                              int gy, int units) {
+  if (p.skip != nullptr && *p.skip != 0) return;  // uniform: before any barrier or allocation
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = reinterpret_cast<uint8_t*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                             ~uintptr_t(1023));
+  uint8_t* sA = smem;
+  uint8_t* sB = smem + STAGES * A_STAGE;
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* tfull = empty + STAGES;   // levels 0..2 of a period are complete
+  uint64_t* tempty = tfull + 1;       // the epilogue has drained levels 0..2
+  uint64_t* tdone = tempty + 1;       // every MMA of the unit is complete
+  uint64_t* tfree = tdone + 1;        // the epilogue has read the unit's levels 3..4
+  uint32_t* tslot = reinterpret_cast<uint32_t*>(tfree + 1);
+  int* abort_flag = reinterpret_cast<int*>(tslot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int G = gridDim.x;
+  auto coords = [&](int u, int& m0, int& n0, int& split, int& k0, int& k1) {
+    n0 = (u % gx) * BN;
+    m0 = ((u / gx) % gy) * BM;
+    split = u / (gx * gy);
+    k0 = split * p.kb_per_split;
+    k1 = min(p.nkb, k0 + p.kb_per_split);
+  };
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(tfull, 1);
+    mbar_init(tempty, EPI_WARPS);
+    mbar_init(tdone, 1);
+    mbar_init(tfree, EPI_WARPS);
+    *abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) {
+    __syncwarp();
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tslot)),
+                 "r"(TMEM_COLS)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tslot;
+
+  if (warp == 0 && lane == 0) {
+    // ---------------- TMA producer: one ring over the K blocks of all units
+    int i = 0, issued = 0;
+    bool stop = false;
+    for (int u = blockIdx.x; u < units && !stop; u += G) {
+      int m0, n0, split, k0, k1;
+      coords(u, m0, n0, split, k0, k1);
+      for (int it = k0; it < k1; ++it, ++i) {
+        const int s = (int)(i % STAGES);
+        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+        if (i >= STAGES && !mbar_wait_or_abort(&empty[s], ph ^ 1u, abort_flag)) {
+          atomicExch(p.err, 1);
+          *(volatile int*)abort_flag = 1;
+          stop = true;
+          break;
+        }
+        if (*(volatile int*)abort_flag) {
+          stop = true;
+          break;
+        }
+        mbar_expect_tx(&full[s], STAGE_BYTES);
+        tma_load_3d(sA + s * A_STAGE, &tmA, it * BK, m0, 0, &full[s]);
+        tma_load_3d(sB + s * B_STAGE, &tmB, it * BK, n0, 0, &full[s]);
+        ++issued;
+      }
+    }
+    if (*(volatile int*)abort_flag) {
+      // drain: let the copies still in flight land before the CTA retires (bounded)
+      for (int j = issued > STAGES ? issued - STAGES : 0; j < issued; ++j)
+        mbar_wait(&full[j % STAGES], (uint32_t)(j / STAGES) & 1u);
+    }
+  } else if (warp == 1 && lane == 0) {
+    // ---------------- MMA issuer (same per-K-block schedule as tc_gemm_kernel; the
+    // period index runs on across units, the first unit after another waits for tfree)
+    int i = 0, Q = 0;
+    int t = 0;
+    bool stop = false;
+    for (int u = blockIdx.x; u < units && !stop; u += G, ++t) {
+      int m0, n0, split, k0, k1;
+      coords(u, m0, n0, split, k0, k1);
+      const int nk = k1 - k0;
+      if (t > 0) {
+        if (!mbar_wait_or_abort(tfree, (uint32_t)(t - 1) & 1u, abort_flag)) {
+          atomicExch(p.err, 2);
+          *(volatile int*)abort_flag = 1;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      }
+      for (int k = 0; k < nk; ++k, ++i) {
+        const int s = (int)(i % STAGES);
+        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+        if (!mbar_wait_or_abort(&full[s], ph, abort_flag)) {
+          atomicExch(p.err, 2);
+          *(volatile int*)abort_flag = 1;
+          stop = true;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
+        const int q = k / FLUSH_KB;
+        const bool period_start = (k % FLUSH_KB) == 0;
+        const bool period_end = ((k + 1) % FLUSH_KB) == 0 || k + 1 == nk;
+        if (period_start && q > 0) {
+          issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, false);
+          if (!mbar_wait_or_abort(tempty, (uint32_t)(Q + q - 1) & 1u, abort_flag)) {
+            atomicExch(p.err, 2);
+            *(volatile int*)abort_flag = 1;
+            umma_commit(&empty[s]);
+            stop = true;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, true);
+          if (period_end) umma_commit(tfull);
+        } else {
+          // a unit's first period: tfree (all of the previous unit's columns read)
+          // covers the drain of that unit's last period
+          issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, period_start);
+          if (period_end) umma_commit(tfull);
+          issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, k == 0);
+        }
+        umma_commit(&empty[s]);
+      }
+      if (stop) break;
+      Q += (nk + FLUSH_KB - 1) / FLUSH_KB;
+      if (nk > 0) umma_commit(tdone);
+      else mbar_arrive(tdone);
+    }
+  } else if (warp >= 2) {
+    // ---------------- epilogue, per unit: exact periods of levels 0..2 -> int64,
+    // levels 3..4 -> FP64 values in registers (then tfree), outputs -> global
+    const int g = warp & 3;
+    const int h = (warp - 2) >> 2;
+    const uint32_t tl = tmem + ((uint32_t)(32 * g) << 16) + (uint32_t)(h * EPI_COLS);
+    int Q = 0;
+    int t = 0;
+    for (int u = blockIdx.x; u < units; u += G, ++t) {
+      int m0, n0, split, k0, k1;
+      coords(u, m0, n0, split, k0, k1);
+      const int nper = (k1 > k0) ? (k1 - k0 + FLUSH_KB - 1) / FLUSH_KB : 0;
+      const int row = m0 + 32 * g + lane;
+      const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
+      // exponents of this warp's EPI_COLS / 2 complex columns, lane c holding column c
+      // (no barrier among the epilogue warps: each reads its own)
+      const int ccol = (n0 >> 1) + h * (EPI_COLS / 2) + lane;
+      const int ebr = (lane < EPI_COLS / 2 && 2 * ccol < p.N) ? p.eb[ccol] : EXP_NONE - 1;
+      long long acc[EPI_COLS];
+#pragma unroll
+      for (int j = 0; j < EPI_COLS; ++j) acc[j] = 0;
+      bool ok = !*(volatile int*)abort_flag;
+      for (int q = 0; q < nper && ok; ++q) {
+        if (!mbar_wait_or_abort(tfull, (uint32_t)(Q + q) & 1u, abort_flag)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int c0 = 0; c0 < EPI_COLS; c0 += 8) {
+          uint32_t v0[8], v1[8], v2[8];
+          __syncwarp();
+          tmem_ld8(tl + (uint32_t)c0, v0);
+          tmem_ld8(tl + (uint32_t)(BN + c0), v1);
+          tmem_ld8(tl + (uint32_t)(2 * BN + c0), v2);
+          tmem_wait_ld();
+          after_wait(v0);
+          after_wait(v1);
+          after_wait(v2);
+          if (c0 + 8 == EPI_COLS) {
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(tempty);
+          }
+#pragma unroll
+          for (int j = 0; j < 8; ++j) acc[c0 + j] += exact_levels(v0[j], v1[j], v2[j]);
+        }
+      }
+      // every unit's tdone phase is consumed, so the parities stay in step
+      if (ok && !mbar_wait_or_abort(tdone, (uint32_t)t & 1u, abort_flag)) ok = false;
+      if (!ok) {
+        if (!*(volatile int*)abort_flag) atomicExch(p.err, 3);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const bool have = nper > 0;
+      // levels 3..4 -> FP64 values (kept in acc as bit patterns), then release TMEM
+#pragma unroll
+      for (int c0 = 0; c0 < EPI_COLS; c0 += 16) {
+        uint32_t v3[16], v4[16];
+        __syncwarp();
+        tmem_ld16(tl + (uint32_t)(3 * BN + c0), v3);
+        tmem_ld16(tl + (uint32_t)(4 * BN + c0), v4);
+        tmem_wait_ld();
+        after_wait(v3);
+        after_wait(v4);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int eb = __shfl_sync(0xffffffffu, ebr, (c0 + j) >> 1);
+          double v = 0.0;
+          if (have && ea > EXP_NONE && eb > EXP_NONE)
+            v = finish_value(acc[c0 + j], v3[j], v4[j], ea + eb - 46);
+          acc[c0 + j] = __double_as_longlong(v);
+        }
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tfree);
+      if (row < p.M) {
+#pragma unroll
+        for (int j = 0; j < EPI_COLS; j += 2) {
+          const int cl = h * EPI_COLS + j;
+          const int col = n0 + cl;
+          if (col >= p.N) break;
+          const double re = __longlong_as_double(acc[j]), im = __longlong_as_double(acc[j + 1]);
+          if (p.part != nullptr) {
+            double2* dst = reinterpret_cast<double2*>(p.part + ((long)split * p.M + row) * p.N + col);
+            *dst = make_double2(re, im);
+          } else {
+            double2* o = p.out + (long)row * p.ldm + (long)(col >> 1) * p.ldn;
+            double2 x = make_double2(re, im);
+            if (p.accumulate) {
+              const double2 y = *o;
+              x.x += y.x;
+              x.y += y.y;
+            }
+            *o = x;
+          }
+        }
+      }
+      Q += nper;
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    __syncwarp();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(TMEM_COLS)
+                 : "memory");
+  }
+}
+
 __global__ void splitk_sum_kernel(const double* __restrict__ part, int splits, int M, int N,
                                   double2* __restrict__ out, long ldm, long ldn, int accumulate,
                                   const int* skip) {
@@ -659,6 +927,8 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* 
   if (!attr) {
     PTN_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       SMEM_BYTES));
+    PTN_CUDA_TRY(cudaFuncSetAttribute(tc_gemm_persistent_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr = true;
   }
   TcArgs a;
@@ -691,7 +961,13 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* 
   PTN_CHECK_ARG(gy <= 65535 && splits <= 65535, "tc_gemm: grid too large");
   const int prof = prof_begin(st, PROF_TC_GEMM, 8.0 * M * (double)Nc * Kc,
                               2.0 * NDIGIT * ((double)M * Kp + (double)N * Kp) + 16.0 * M * Nc);
-  tc_gemm_kernel<<<dim3(gx, gy, splits), THREADS, SMEM_BYTES, st>>>(ma, mb, a);
+  const long units = (long)gx * gy * splits;
+  if (tune(PTN_TUNE_TC_PERSISTENT) != 0 && units <= INT_MAX) {
+    const int grid = (int)std::min<long>(units, num_sms());
+    tc_gemm_persistent_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, a, gx, gy, (int)units);
+  } else {
+    tc_gemm_kernel<<<dim3(gx, gy, splits), THREADS, SMEM_BYTES, st>>>(ma, mb, a);
+  }
   PTN_LAUNCH_CHECK();
   note_launches(1);
   if (splits > 1) {

@@ -46,6 +46,9 @@ def test_tuning_knobs_validate_and_round_trip():
         assert L.ptn_tune_set(k, v) == _lib.PTN_OK and L.ptn_tune_get(k) == v
         assert L.ptn_tune_set(k, old) == _lib.PTN_OK
     assert L.ptn_tune_set(_lib.TUNE_LARFB_TILE, 9) == _lib.PTN_BAD_SHAPE
+    assert L.ptn_tune_set(_lib.TUNE_QR_PANEL, 4) == _lib.PTN_BAD_SHAPE
+    assert L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, 2) == _lib.PTN_BAD_SHAPE
+    assert L.ptn_tune_get(_lib.TUNE_QR_PANEL) == 0 and L.ptn_tune_get(_lib.TUNE_TC_PERSISTENT) == 1
     assert L.ptn_tune_set(7, 1) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES) == 1
 

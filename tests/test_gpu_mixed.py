@@ -58,6 +58,30 @@ def test_split_bf16_gemm(ptg, mnk):
     assert err < 1e-10, err
 
 
+@pytest.mark.parametrize("mnk", [(7, 5, 3), (1024, 2560, 512), (512, 1024, 2560),
+                                 (300, 257, 3000), (2048, 1024, 1024)])
+def test_persistent_gemm_equals_one_cta_per_tile(ptg, mnk):
+    """PTN_TUNE_TC_PERSISTENT 1 (one CTA per SM over all (tile, K split) units) and 0
+    (one CTA per unit) run the same per-unit arithmetic: bit-identical results,
+    also with several units per CTA and K splits."""
+    from pytenet_gb300 import _lib
+    L = _lib.load()
+    M, N, K = mnk
+    rng = np.random.default_rng(M + 5 * N + 11 * K)
+    A = orc.crandn((M, K), rng)
+    B = orc.crandn((K, N), rng)
+    old = L.ptn_tune_get(_lib.TUNE_TC_PERSISTENT)
+    try:
+        assert L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, 1) == 0
+        C1 = split_gemm(A, B)
+        assert L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, 0) == 0
+        C0 = split_gemm(A, B)
+    finally:
+        L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, old)
+    assert np.array_equal(C1, C0)
+    assert rel(C1, A @ B) < 1e-10
+
+
 def test_split_bf16_gemm_zero_rows_and_scales(ptg):
     """All-zero rows / columns (block-sparse tensors) and rows of very different
     magnitude: each row carries its own power-of-two scale."""
