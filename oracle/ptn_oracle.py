@@ -31,7 +31,8 @@ __all__ = [
     "apply_local_hamiltonian", "apply_local_bond_contraction",
     "mpo_inner_product", "mpo_average",
     "lanczos_iteration", "eigh_tridiag", "expm_krylov", "eigh_krylov",
-    "tdvp_singlesite", "dmrg_singlesite",
+    "tdvp_singlesite", "dmrg_singlesite", "compress_svd", "compress_density",
+    "block_sparse_eigh",
 ]
 
 
@@ -742,3 +743,79 @@ def compress_svd(psi, tol, direction="left"):
         psi.a[0] = psi.a[0] * (t[0, 0, 0] / abs(t[0, 0, 0]))
         return nrm, abs(t[0, 0, 0])
     raise ValueError(f'`direction` = {direction} invalid; must be "left" or "right".')
+
+
+# ---------------------------------------------------------------------------
+# compression from local density matrices -- pytenet/mps.py:238-290 (McCulloch,
+# J. Stat. Mech. (2007) P10014), with block_sparse_eigh from
+# pytenet/block_sparse_util.py:183-241 and the left partial contractions of
+# pytenet/mps.py:384-427
+# ---------------------------------------------------------------------------
+
+def block_sparse_eigh(a, q0):
+    """Hermitian eigendecomposition per quantum-number block of `a` (rows and
+    columns carry q0), block_sparse_util.py:183-241: the blocks in the iteration
+    order of the Python set of q0, eigenvalues ascending inside a block (LAPACK
+    heevd), rows of u in the input order. Returns (u, evals, q)."""
+    a = np.asarray(a)
+    q0 = np.asarray(q0)
+    order = list(set(q0))                      # the reference iterates set(q0)
+    a_s, (idx0, q0s), (_, q1s) = sort_by_qnumbers(a, q0, q0)
+    n = a_s.shape[0]
+    u = np.zeros((n, n), dtype=a.dtype)
+    ev = np.zeros(n)
+    q = np.zeros(n, dtype=q0.dtype)
+    k = 0
+    for qn in order:
+        rs, cs = _qslice(qn, q0s), _qslice(qn, q1s)
+        w, v = np.linalg.eigh(a_s[rs, cs])
+        u[rs, k:k + len(w)] = v
+        ev[k:k + len(w)] = w
+        q[k:k + len(w)] = qn
+        k += len(w)
+    u, ev, q = u[:, :k], ev[:k], q[:k]
+    if np.any(idx0 - np.arange(len(idx0))):
+        u = u[np.argsort(idx0), :]
+    return u, ev, q
+
+
+def mps_left_blocks(psi):
+    """Left partial contractions of <psi|psi> (mps.py:384-427): blocks[0] = [[1]],
+    blocks[i+1][r, r'] = sum a_i[l, s, r] (blocks[i] conj(a_i))[l, s, r']."""
+    blocks = [np.identity(1, dtype=psi.a[0].dtype)]
+    for a in psi.a:
+        t = np.tensordot(blocks[-1], a.conj(), axes=(1, 0))
+        blocks.append(np.tensordot(a, t, axes=((0, 1), (0, 1))))
+    return blocks
+
+
+def compress_density(psi, tol):
+    """Rounding compression from local density matrices, right to left, in place
+    (mps.py:238-290); returns (original norm, scaling factor of the compression)."""
+    n = len(psi.a)
+    lb = mps_left_blocks(psi)
+    assert lb[-1].shape == (1, 1) and lb[-1][0, 0].real > 0
+    nrm = np.sqrt(lb[-1][0, 0].real)
+    b = np.array([[[1]]], dtype=psi.a[-1].dtype)
+    u = np.array([[[1]]], dtype=psi.a[-1].dtype)
+    for i in reversed(range(1, n)):
+        b = np.tensordot(b, u.conj(), axes=((1, 2), (1, 2)))
+        b = np.tensordot(psi.a[i], b, axes=((2,), (0,)))
+        rho = np.tensordot(b, lb[i], axes=((0,), (0,)))
+        rho = np.tensordot(rho, b.conj(), axes=((2,), (0,)))
+        shp = rho.shape[:2]
+        rho = rho.reshape((shp[0] * shp[1], -1))
+        qr = qnumber_flatten((psi.qsite, -np.asarray(psi.qbonds[i + 1])))
+        assert is_qsparse(rho, (qr, -qr))
+        u, ev, qe = block_sparse_eigh(rho, qr)
+        idx = retained_bond_indices(np.abs(ev), tol)   # eigenvalues can be slightly negative
+        u = u[:, idx]
+        qe = -qe[idx]
+        u = u.reshape(shp[0], shp[1], u.shape[1]).transpose((2, 0, 1))
+        psi.a[i] = u
+        psi.qbonds[i] = qe
+    b = np.tensordot(b, u.conj(), axes=((1, 2), (1, 2)))
+    b = np.tensordot(psi.a[0], b, axes=((2,), (0,)))
+    s = np.linalg.norm(b.reshape(-1))
+    psi.a[0] = b / s
+    return nrm, s / nrm

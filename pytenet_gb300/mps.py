@@ -114,16 +114,16 @@ class MPS:
         return float(nrm.item())
 
     def compress(self, tol, mode="svd", direction="left"):
-        """Compress and orthonormalise by site-local truncated SVDs on the GPU;
-        returns the original norm and the scaling factor of the compression
-        (pytenet/mps.py:180-236). The reference's "density" mode (rounding by local
-        density matrices, pytenet/mps.py:238-290) is not part of this engine."""
+        """Compress and orthonormalise on the GPU, by site-local truncated SVDs
+        (mode "svd", pytenet/mps.py:180-236) or by rounding with local density
+        matrices (mode "density", right to left, pytenet/mps.py:238-290); returns
+        the original norm and the scaling factor of the compression."""
         if mode == "svd":
             from .compression import compress_svd
             return compress_svd(self, tol, direction)
         if mode == "density":
-            raise NotImplementedError('compress(mode="density") is not provided by pytenet_gb300; '
-                                      'use mode="svd"')
+            from .compression import compress_density
+            return compress_density(self, tol)
         raise ValueError(f'`mode` = {mode} invalid; must be "svd" or "density".')
 
     def to_vector(self):

@@ -295,8 +295,9 @@ def gen_twosite():
 
 
 def gen_compress():
-    """MPS.compress(tol, "svd", direction) (mps.py:180-236) on an MPS with quantum
-    numbers whose bonds carry more than the state needs: an MPO applied to a state."""
+    """MPS.compress(tol, "svd", direction) (mps.py:180-236) and MPS.compress(tol,
+    "density") (mps.py:238-290) on an MPS with quantum numbers whose bonds carry
+    more than the state needs: an MPO applied to a state."""
     rng = np.random.default_rng(1014)
     nsites = 7
     h = ptn.heisenberg_xxz_1d_mpo(nsites, 1.0, 0.8, -0.1)
@@ -313,6 +314,12 @@ def gen_compress():
         out.update(pack_mps(f"{direction}_", p))
         out[f"{direction}_nrm"] = np.array(nrm)
         out[f"{direction}_scale"] = np.array(scale)
+    p = copy.deepcopy(psi)
+    nrm, scale = p.compress(1e-6, mode="density")
+    out.update(pack_mps("density_", p))
+    out["density_nrm"] = np.array(nrm)
+    out["density_scale"] = np.array(scale)
+    out["density_v"] = p.to_vector()
     save("compress.npz", **out)
 
 

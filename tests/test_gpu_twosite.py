@@ -222,3 +222,29 @@ def test_compress_svd_matches_reference(ptg):
         print("compress", direction, "bonds", [len(q) for q in psi.qbonds], "state",
               np.abs(v - vr).max())
         assert np.abs(v - vr).max() < 1e-10 * max(1.0, np.abs(vr).max())
+
+
+def test_compress_density_matches_reference(ptg):
+    """MPS.compress(tol, "density") on the device (pytenet/mps.py:238-290): density
+    matrices from FP64 GEMMs, eigenvectors per quantum-number block from the device
+    SVD in the reference's block and eigenvalue order. Against the reference
+    fixture: bond dimensions and quantum numbers bit-exact, norm and compression
+    factor to 1e-12, the compressed state to 1e-10; the svd and density results
+    describe states of the same norm."""
+    g = load_golden("compress.npz")
+    p0 = golden_mps(g, "p0_")
+    psi = ptg.MPS(p0.qsite, p0.qbonds, fill="postpone")
+    psi.a = [x.copy() for x in p0.a]
+    nrm, scale = psi.compress(1e-6, mode="density")
+    ref = golden_mps(g, "density_")
+    assert abs(nrm - float(g["density_nrm"])) < 1e-12 * abs(float(g["density_nrm"]))
+    assert abs(scale - float(g["density_scale"])) < 1e-12
+    for qa, qb in zip(psi.qbonds, ref.qbonds):
+        assert np.array_equal(qa, qb)
+    for x, y in zip(psi.a, ref.a):
+        assert x.shape == y.shape
+    v = psi_vector(psi)
+    vr = g["density_v"]
+    print("compress density bonds", [len(q) for q in psi.qbonds], "state", np.abs(v - vr).max())
+    assert np.abs(v - vr).max() < 1e-10 * max(1.0, np.abs(vr).max())
+    assert abs(np.linalg.norm(v) - 1.0) < 1e-12

@@ -229,6 +229,26 @@ def test_compress_svd_matches_reference():
             assert np.allclose(x, y, rtol=0, atol=1e-10)
 
 
+def test_compress_density_matches_reference():
+    """MPS.compress(tol, "density") (mps.py:238-290, block_sparse_eigh of
+    block_sparse_util.py:183-241): bond dimensions and quantum numbers bit-exact
+    (blocks in the order of the Python set of the row quantum numbers), tensors,
+    norm and scale to 1e-12."""
+    g = load_golden("compress.npz")
+    psi = golden_mps(g, "p0_")
+    nrm, scale = orc.compress_density(psi, 1e-6)
+    ref = golden_mps(g, "density_")
+    assert abs(nrm - float(g["density_nrm"])) < 1e-12 * abs(float(g["density_nrm"]))
+    assert abs(scale - float(g["density_scale"])) < 1e-12
+    assert [len(q) for q in psi.qbonds] != [len(q) for q in golden_mps(g, "p0_").qbonds]
+    for qa, qb in zip(psi.qbonds, ref.qbonds):
+        assert np.array_equal(qa, qb)
+    for x, y in zip(psi.a, ref.a):
+        assert x.shape == y.shape
+        assert np.allclose(x, y, rtol=0, atol=1e-12)
+    assert np.allclose(orc.mps_to_vector(psi), g["density_v"], rtol=0, atol=1e-12)
+
+
 def test_xxz_l64_fixture_input_and_initial_state():
     """The L=64, D=256 fixture (whole trajectory checked on the GPU): its input is
     regenerated from the seed with the reference's draw order, bit for bit, and
