@@ -113,6 +113,12 @@ uint64_t ptn_launch_count(void);
  *   PTN_TUNE_TC_PERSISTENT     1 (default): the tensor-core GEMM runs one CTA per SM over
  *                              all (tile, K split) units, the next unit's loads and MMAs
  *                              overlapping the current one's epilogue; 0: one CTA per unit.
+ *   PTN_TUNE_TC_SKIP_ZERO      1: the digit conversion flags the all-zero (tile, K block)
+ *                              cells of each operand and the persistent GEMM skips them
+ *                              (quantum-number block sparsity, exact); 0 (default): every
+ *                              block is multiplied (the flags cost ~5 % on dense data and
+ *                              the 128 x 96 tiles are coarser than the sectors at bonds
+ *                              up to 256).
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,
@@ -122,7 +128,8 @@ enum {
   PTN_TUNE_KRYLOV_FUSED = 4,
   PTN_TUNE_QR_PANEL = 5,
   PTN_TUNE_TC_PERSISTENT = 6,
-  PTN_TUNE_COUNT = 7
+  PTN_TUNE_TC_SKIP_ZERO = 7,
+  PTN_TUNE_COUNT = 8
 };
 ptn_status ptn_tune_set(int key, int value);
 int ptn_tune_get(int key);

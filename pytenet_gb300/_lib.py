@@ -21,6 +21,7 @@ TUNE_TC_SPLIT_WAVES, TUNE_ZGEMM_SPLIT_WAVES, TUNE_LARFB_TILE, TUNE_QR_CLUSTER = 
 TUNE_KRYLOV_FUSED = 4
 TUNE_QR_PANEL = 5
 TUNE_TC_PERSISTENT = 6
+TUNE_TC_SKIP_ZERO = 7
 
 
 class PtnError(RuntimeError):

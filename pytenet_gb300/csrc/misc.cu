@@ -24,8 +24,8 @@ void set_error(const char* fmt, ...) {
 void note_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
 namespace {
-std::atomic<int> g_tune[PTN_TUNE_COUNT] = {{1}, {2}, {0}, {0}, {1}, {0}, {1}};
-constexpr int kTuneMax[PTN_TUNE_COUNT] = {16, 16, 5, 16, 1, 3, 1};
+std::atomic<int> g_tune[PTN_TUNE_COUNT] = {{1}, {2}, {0}, {0}, {1}, {0}, {1}, {0}};
+constexpr int kTuneMax[PTN_TUNE_COUNT] = {16, 16, 5, 16, 1, 3, 1, 1};
 }  // namespace
 
 int tune(int key) { return (key >= 0 && key < PTN_TUNE_COUNT) ? g_tune[key].load() : 0; }

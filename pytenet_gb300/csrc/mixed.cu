@@ -31,7 +31,8 @@ namespace ptn {
 void note_launches(int n);
 ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* Bslices, long bplane,
                    const int* eb, int M, int Nc, int Kc, long Kp, double2* out, long ldm, long ldn,
-                   bool accumulate, void* ws, size_t ws_bytes, const int* skip, cudaStream_t st);
+                   bool accumulate, void* ws, size_t ws_bytes, const int* skip, cudaStream_t st,
+                   const unsigned char* fa, const unsigned char* fb, int fk);
 size_t tc_gemm_workspace_bytes(int M, int Ncomplex, int Kcomplex);
 ptn_status mpo_stage_f64(const double2* in, double2* out, const double2* w, long ldq, long ldp, int X,
                          int P, int Q, int Y, const int* skip, cudaStream_t st);
@@ -114,14 +115,33 @@ __device__ __forceinline__ void digits_of(double x, int ex, bf16 (&d)[NDIGIT]) {
   d[0] = __int2bfloat16_rn((int)T);
 }
 
+// With zero-tile flags on (flags_on), also marks flags[1 + (r / fg) * fk + k / 16]
+// for every non-zero entry (r, k): the tiles of the digit GEMM (128 rows of a plain
+// operand, 48 complex columns of an embedded one) by K block of 16 complex entries,
+// so that the GEMM can skip all-zero tiles (quantum-number block sparsity); one
+// store per warp, row and K block (the buffer is zeroed before). flags[0] tells the
+// GEMM whether the flags of this conversion are valid.
 __global__ void digits_kernel(const double2* __restrict__ src, long sr, long sk, int R, int K,
                               int conj, const int* __restrict__ e, bf16* __restrict__ dst, long Kp,
-                              long plane, int embedded, const int* skip) {
+                              long plane, int embedded, unsigned char* __restrict__ flags,
+                              int flags_on, int fg, long fk, const int* skip) {
   if (skip != nullptr && *skip != 0) return;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0)
+    flags[0] = (unsigned char)flags_on;
   __shared__ double2 tile[32][33];
   const int r0 = blockIdx.y * 32, k0 = blockIdx.x * 32;
   load_tile(tile, src, sr, sk, R, K, r0, k0, conj);
   __syncthreads();
+  if (flags_on) {
+    // lanes 0..15 and 16..31 of a row cover one K block each
+    for (int rr = threadIdx.y; rr < 32; rr += 8) {
+      const int r = r0 + rr, k = k0 + threadIdx.x;
+      const double2 z = tile[rr][threadIdx.x];
+      const unsigned nz = __ballot_sync(0xffffffffu, r < R && k < K && (z.x != 0.0 || z.y != 0.0));
+      const unsigned half = (threadIdx.x < 16) ? (nz & 0xFFFFu) : (nz >> 16);
+      if ((threadIdx.x & 15) == 0 && half != 0) flags[1 + (long)(r / fg) * fk + (k >> 4)] = 1;
+    }
+  }
   const int k = k0 + threadIdx.x;
   if (k >= K) return;
   for (int rr = threadIdx.y; rr < 32; rr += 8) {
@@ -189,8 +209,12 @@ size_t before_gemm(const Carver& c, const W& w) {
 struct Digits {
   bf16* p;
   int* e;
+  unsigned char* f;   // non-zero flags per (GEMM tile of rows, K block of 16 complex)
   long rows, kc, Kp;
   bool embedded;
+  int fgroup() const { return embedded ? 48 : 128; }
+  long fk() const { return (kc + 15) / 16; }
+  long frows() const { return (rows + fgroup() - 1) / fgroup(); }
   long real_rows() const { return embedded ? 2 * rows : rows; }
   long plane() const { return real_rows() * Kp; }
 };
@@ -203,6 +227,7 @@ Digits take_digits(Carver& c, long rows, long kc, bool embedded) {
   d.embedded = embedded;
   d.p = static_cast<bf16*>(c.take((size_t)NDIGIT * d.real_rows() * d.Kp * sizeof(bf16)));
   d.e = static_cast<int*>(c.take((size_t)rows * sizeof(int)));
+  d.f = static_cast<unsigned char*>(c.take(1 + (size_t)d.frows() * d.fk()));
   return d;
 }
 
@@ -210,11 +235,14 @@ Digits take_digits(Carver& c, long rows, long kc, bool embedded) {
 ptn_status to_digits(const double2* src, long sr, long sk, const Digits& d, bool conj,
                      const int* skip, cudaStream_t st) {
   PTN_CUDA_TRY(cudaMemsetAsync(d.e, 0x80, (size_t)d.rows * sizeof(int), st));
+  const int flags_on = tune(PTN_TUNE_TC_SKIP_ZERO) != 0 ? 1 : 0;
+  if (flags_on) PTN_CUDA_TRY(cudaMemsetAsync(d.f, 0, 1 + (size_t)d.frows() * d.fk(), st));
   dim3 grid((unsigned)((d.kc + 31) / 32), (unsigned)((d.rows + 31) / 32));
   PTN_CHECK_ARG(grid.y <= 65535, "digits: too many rows");
   rowexp_kernel<<<grid, dim3(32, 8), 0, st>>>(src, sr, sk, (int)d.rows, (int)d.kc, d.e, skip);
   digits_kernel<<<grid, dim3(32, 8), 0, st>>>(src, sr, sk, (int)d.rows, (int)d.kc, conj ? 1 : 0,
-                                              d.e, d.p, d.Kp, d.plane(), d.embedded ? 1 : 0, skip);
+                                              d.e, d.p, d.Kp, d.plane(), d.embedded ? 1 : 0, d.f,
+                                              flags_on, d.fgroup(), d.fk(), skip);
   PTN_LAUNCH_CHECK();
   note_launches(2);
   return PTN_OK;
@@ -223,8 +251,10 @@ ptn_status to_digits(const double2* src, long sr, long sk, const Digits& d, bool
 // C = A . B^T over the digit planes: A plain (M x Kc), B embedded (Nc x Kc)
 ptn_status gemm(const Digits& A, const Digits& Be, double2* out, long ldm, long ldn, void* ws,
                 size_t ws_bytes, const int* skip, cudaStream_t st) {
+  const bool flags = tune(PTN_TUNE_TC_SKIP_ZERO) != 0;
   return tc_gemm(A.p, A.plane(), A.e, Be.p, Be.plane(), Be.e, (int)A.rows, (int)Be.rows,
-                 (int)A.kc, A.Kp, out, ldm, ldn, false, ws, ws_bytes, skip, st);
+                 (int)A.kc, A.Kp, out, ldm, ldn, false, ws, ws_bytes, skip, st,
+                 flags ? A.f : nullptr, flags ? Be.f : nullptr, (int)A.fk());
 }
 
 // ---------------------------------------------------------------- H_eff (site)

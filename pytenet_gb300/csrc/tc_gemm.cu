@@ -103,6 +103,13 @@ struct TcArgs {
   double* part;        // split-K partials [splits][M][N], or null
   int* err;
   const int* skip;
+  // non-zero flags of (128-row tile of A, K block) and (96-row tile of B, K block),
+  // fk K blocks per row of flags after a validity byte, or null: the persistent
+  // kernel skips every K block where either operand tile is zero (exact: those
+  // products are zero); flags whose validity byte is 0 are ignored
+  const unsigned char* fa;
+  const unsigned char* fb;
+  int fk;
 };
 
 // digit pairs, grouped by level; the first pair of each level starts its accumulator
@@ -251,6 +258,27 @@ __device__ __forceinline__ double finish_value(long long x, uint32_t a3, uint32_
   const int e = (int)((b >> 52) & 0x7FF) + sh;
   if (e > 0 && e < 2047) return __longlong_as_double(b + ((long long)sh << 52));
   return ldexp(r, sh);
+}
+
+// K blocks [k0, k1) of a unit (at most MAX_K_SPLIT / BK = 128) that have both
+// operand tiles non-zero, as four 32-bit masks; all lanes of the warp take part
+__device__ __forceinline__ int unit_mask(const TcArgs& p, int m0, int n0, int k0, int k1, int lane,
+                                         uint32_t (&mk)[4]) {
+  int n = 0;
+#pragma unroll
+  for (int w = 0; w < 4; ++w) {
+    const int k = k0 + w * 32 + lane;
+    bool act = k < k1;
+    if (act && p.fa != nullptr && p.fa[0] != 0 && p.fb[0] != 0)
+      act = p.fa[1 + (long)(m0 / BM) * p.fk + k] != 0 && p.fb[1 + (long)(n0 / BN) * p.fk + k] != 0;
+    mk[w] = __ballot_sync(0xffffffffu, act);
+    n += __popc(mk[w]);
+  }
+  return n;
+}
+
+__device__ __forceinline__ bool mask_bit(const uint32_t (&mk)[4], int j) {
+  return (mk[j >> 5] >> (j & 31)) & 1u;
 }
 
 // the MMAs of digit pairs [P0, P1) of one K block (stage addresses a0 / b0); the
@@ -556,94 +584,113 @@ __global__ void __launch_bounds__(THREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tslot;
 
-  if (warp == 0 && lane == 0) {
-    // ---------------- TMA producer: one ring over the K blocks of all units
+  if (warp == 0) {
+    // ---------------- TMA producer (lane 0): one ring over the active K blocks of all
+    // units; the whole warp forms each unit's mask
     int i = 0, issued = 0;
     bool stop = false;
     for (int u = blockIdx.x; u < units && !stop; u += G) {
       int m0, n0, split, k0, k1;
       coords(u, m0, n0, split, k0, k1);
-      for (int it = k0; it < k1; ++it, ++i) {
-        const int s = (int)(i % STAGES);
-        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (i >= STAGES && !mbar_wait_or_abort(&empty[s], ph ^ 1u, abort_flag)) {
-          atomicExch(p.err, 1);
-          *(volatile int*)abort_flag = 1;
-          stop = true;
-          break;
+      uint32_t mk[4];
+      unit_mask(p, m0, n0, k0, k1, lane, mk);
+      if (lane == 0) {
+        for (int it = k0; it < k1; ++it) {
+          if (!mask_bit(mk, it - k0)) continue;
+          const int s = i % STAGES;
+          const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+          if (i >= STAGES && !mbar_wait_or_abort(&empty[s], ph ^ 1u, abort_flag)) {
+            atomicExch(p.err, 1);
+            *(volatile int*)abort_flag = 1;
+            stop = true;
+            break;
+          }
+          if (*(volatile int*)abort_flag) {
+            stop = true;
+            break;
+          }
+          mbar_expect_tx(&full[s], STAGE_BYTES);
+          tma_load_3d(sA + s * A_STAGE, &tmA, it * BK, m0, 0, &full[s]);
+          tma_load_3d(sB + s * B_STAGE, &tmB, it * BK, n0, 0, &full[s]);
+          ++issued;
+          ++i;
         }
-        if (*(volatile int*)abort_flag) {
-          stop = true;
-          break;
-        }
-        mbar_expect_tx(&full[s], STAGE_BYTES);
-        tma_load_3d(sA + s * A_STAGE, &tmA, it * BK, m0, 0, &full[s]);
-        tma_load_3d(sB + s * B_STAGE, &tmB, it * BK, n0, 0, &full[s]);
-        ++issued;
       }
+      stop = __shfl_sync(0xffffffffu, stop ? 1 : 0, 0) != 0;
     }
-    if (*(volatile int*)abort_flag) {
+    if (lane == 0 && *(volatile int*)abort_flag) {
       // drain: let the copies still in flight land before the CTA retires (bounded)
       for (int j = issued > STAGES ? issued - STAGES : 0; j < issued; ++j)
         mbar_wait(&full[j % STAGES], (uint32_t)(j / STAGES) & 1u);
     }
-  } else if (warp == 1 && lane == 0) {
-    // ---------------- MMA issuer (same per-K-block schedule as tc_gemm_kernel; the
-    // period index runs on across units, the first unit after another waits for tfree)
-    int i = 0, Q = 0;
-    int t = 0;
+  } else if (warp == 1) {
+    // ---------------- MMA issuer (lane 0; same per-K-block schedule as tc_gemm_kernel
+    // over the unit's active K blocks; the period index runs on across units, the
+    // first unit after another waits for tfree)
+    int i = 0, Q = 0, t = 0;
     bool stop = false;
     for (int u = blockIdx.x; u < units && !stop; u += G, ++t) {
       int m0, n0, split, k0, k1;
       coords(u, m0, n0, split, k0, k1);
-      const int nk = k1 - k0;
-      if (t > 0) {
-        if (!mbar_wait_or_abort(tfree, (uint32_t)(t - 1) & 1u, abort_flag)) {
-          atomicExch(p.err, 2);
-          *(volatile int*)abort_flag = 1;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      }
-      for (int k = 0; k < nk; ++k, ++i) {
-        const int s = (int)(i % STAGES);
-        const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
-        if (!mbar_wait_or_abort(&full[s], ph, abort_flag)) {
-          atomicExch(p.err, 2);
-          *(volatile int*)abort_flag = 1;
-          stop = true;
-          break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
-        const int q = k / FLUSH_KB;
-        const bool period_start = (k % FLUSH_KB) == 0;
-        const bool period_end = ((k + 1) % FLUSH_KB) == 0 || k + 1 == nk;
-        if (period_start && q > 0) {
-          issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, false);
-          if (!mbar_wait_or_abort(tempty, (uint32_t)(Q + q - 1) & 1u, abort_flag)) {
+      uint32_t mk[4];
+      const int nk = unit_mask(p, m0, n0, k0, k1, lane, mk);
+      if (lane == 0) {
+        bool ok = true;
+        if (t > 0) {
+          if (!mbar_wait_or_abort(tfree, (uint32_t)(t - 1) & 1u, abort_flag)) {
             atomicExch(p.err, 2);
             *(volatile int*)abort_flag = 1;
-            umma_commit(&empty[s]);
-            stop = true;
+            ok = false;
+          } else {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          }
+        }
+        for (int it = k0, k = 0; ok && it < k1; ++it) {
+          if (!mask_bit(mk, it - k0)) continue;
+          const int s = i % STAGES;
+          const uint32_t ph = (uint32_t)(i / STAGES) & 1u;
+          if (!mbar_wait_or_abort(&full[s], ph, abort_flag)) {
+            atomicExch(p.err, 2);
+            *(volatile int*)abort_flag = 1;
+            ok = false;
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, true);
-          if (period_end) umma_commit(tfull);
-        } else {
-          // a unit's first period: tfree (all of the previous unit's columns read)
-          // covers the drain of that unit's last period
-          issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, period_start);
-          if (period_end) umma_commit(tfull);
-          issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, k == 0);
+          const uint32_t a0 = smem_u32(sA + s * A_STAGE), b0 = smem_u32(sB + s * B_STAGE);
+          const int q = k / FLUSH_KB;
+          const bool period_start = (k % FLUSH_KB) == 0;
+          const bool period_end = ((k + 1) % FLUSH_KB) == 0 || k + 1 == nk;
+          if (period_start && q > 0) {
+            issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, false);
+            if (!mbar_wait_or_abort(tempty, (uint32_t)(Q + q - 1) & 1u, abort_flag)) {
+              atomicExch(p.err, 2);
+              *(volatile int*)abort_flag = 1;
+              umma_commit(&empty[s]);
+              ok = false;
+              break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, true);
+            if (period_end) umma_commit(tfull);
+          } else {
+            // a unit's first period: tfree (all of the previous unit's columns read)
+            // covers the drain of that unit's last period
+            issue_pairs<0, EXACT_PAIRS>(tmem, a0, b0, period_start);
+            if (period_end) umma_commit(tfull);
+            issue_pairs<EXACT_PAIRS, NPAIR>(tmem, a0, b0, k == 0);
+          }
+          umma_commit(&empty[s]);
+          ++k;
+          ++i;
         }
-        umma_commit(&empty[s]);
+        if (ok) {
+          Q += (nk + FLUSH_KB - 1) / FLUSH_KB;
+          if (nk > 0) umma_commit(tdone);
+          else mbar_arrive(tdone);
+        }
+        stop = !ok;
       }
-      if (stop) break;
-      Q += (nk + FLUSH_KB - 1) / FLUSH_KB;
-      if (nk > 0) umma_commit(tdone);
-      else mbar_arrive(tdone);
+      stop = __shfl_sync(0xffffffffu, stop ? 1 : 0, 0) != 0;
     }
   } else if (warp >= 2) {
     // ---------------- epilogue, per unit: exact periods of levels 0..2 -> int64,
@@ -656,7 +703,8 @@ __global__ void __launch_bounds__(THREADS, 1)
     for (int u = blockIdx.x; u < units; u += G, ++t) {
       int m0, n0, split, k0, k1;
       coords(u, m0, n0, split, k0, k1);
-      const int nper = (k1 > k0) ? (k1 - k0 + FLUSH_KB - 1) / FLUSH_KB : 0;
+      uint32_t mk[4];
+      const int nper = (unit_mask(p, m0, n0, k0, k1, lane, mk) + FLUSH_KB - 1) / FLUSH_KB;
       const int row = m0 + 32 * g + lane;
       const int ea = (row < p.M) ? p.ea[row] : EXP_NONE - 1;
       // exponents of this warp's EPI_COLS / 2 complex columns, lane c holding column c
@@ -910,9 +958,13 @@ size_t tc_gemm_workspace_bytes(int M, int Ncomplex, int Kcomplex) {
 // C (M x Nc complex) = A (M x Kc) * B (Kc x Nc) from digit planes:
 //   Aslices: [5][M][Kp] BF16 (plain) with row exponents ea[M],
 //   Bslices: [5][2 Nc][Kp] BF16 (embedded) with exponents eb[Nc]; Kp >= 2 Kc, Kp % 8 == 0.
+//   fa / fb (or null): a validity byte, then non-zero flags per (128-row tile of A,
+//   K block of 16 complex) and (48-column tile of B, K block), fk K blocks per flag
+//   row; K blocks where either tile is zero are skipped by the persistent kernel.
 ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* Bslices, long bplane,
                    const int* eb, int M, int Nc, int Kc, long Kp, double2* out, long ldm, long ldn,
-                   bool accumulate, void* ws, size_t ws_bytes, const int* skip, cudaStream_t st) {
+                   bool accumulate, void* ws, size_t ws_bytes, const int* skip, cudaStream_t st,
+                   const unsigned char* fa, const unsigned char* fb, int fk) {
   const int N = 2 * Nc, K = 2 * Kc;
   PTN_CHECK_ARG(M > 0 && Nc > 0 && Kc > 0 && Kp >= K && Kp % 8 == 0, "tc_gemm: bad sizes");
   PTN_CHECK_ARG(reinterpret_cast<uintptr_t>(Aslices) % 16 == 0 &&
@@ -957,6 +1009,11 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* 
   a.part = splits > 1 ? static_cast<double*>(ws) : nullptr;
   a.err = err_flag();
   a.skip = skip;
+  const bool flags = fa != nullptr && fb != nullptr;
+  PTN_CHECK_ARG(!flags || fk == a.nkb, "tc_gemm: flag rows of %d K blocks for %d", fk, a.nkb);
+  a.fa = flags ? fa : nullptr;
+  a.fb = flags ? fb : nullptr;
+  a.fk = fk;
   PTN_CHECK_ARG(a.err != nullptr, "tc_gemm: error flag lookup failed");
   PTN_CHECK_ARG(gy <= 65535 && splits <= 65535, "tc_gemm: grid too large");
   const int prof = prof_begin(st, PROF_TC_GEMM, 8.0 * M * (double)Nc * Kc,
