@@ -52,7 +52,7 @@ typedef enum {
 
 typedef struct { double re, im; } ptn_c128;
 
-#define PTN_ABI_VERSION 2
+#define PTN_ABI_VERSION 3
 #define PTN_KRYLOV_MAXITER 64
 
 /* Device-resident state of one Krylov (Lanczos) run. Laid out for direct reads

@@ -30,7 +30,7 @@ def test_library_exports_every_header_symbol():
     from pytenet_gb300 import _lib
     assert set(_lib.exported_names()) == set(syms)
     L = _lib.load(path)
-    assert L.ptn_abi_version() == _lib.ABI_VERSION == 2
+    assert L.ptn_abi_version() == _lib.ABI_VERSION == 3
     assert b"sm_103a" in L.ptn_version()
 
 
