@@ -110,15 +110,16 @@ uint64_t ptn_launch_count(void);
  *                              3 the same layout with a shuffle reduce-scatter; 1 the
  *                              earlier one-warp-per-row-group panel; 2 that panel with
  *                              the reflector scalars and the cluster gather in one warp.
- *   PTN_TUNE_TC_PERSISTENT     1 (default): the tensor-core GEMM runs one CTA per SM over
- *                              all (tile, K split) units, the next unit's loads and MMAs
- *                              overlapping the current one's epilogue; 0: one CTA per unit.
+ *   PTN_TUNE_TC_PERSISTENT     0 (default): the tensor-core GEMM runs one CTA per (tile,
+ *                              K split) unit; 1: one CTA per SM over all units, the next
+ *                              unit's loads and MMAs overlapping the current one's
+ *                              epilogue (same results bit for bit; measured slower on
+ *                              dense data).
  *   PTN_TUNE_TC_SKIP_ZERO      1: the digit conversion flags the all-zero (tile, K block)
- *                              cells of each operand and the persistent GEMM skips them
- *                              (quantum-number block sparsity, exact); 0 (default): every
- *                              block is multiplied (the flags cost ~5 % on dense data and
- *                              the 128 x 96 tiles are coarser than the sectors at bonds
- *                              up to 256).
+ *                              cells of each operand and the GEMM (persistent form) skips
+ *                              them (quantum-number block sparsity, exact); 0 (default):
+ *                              every block is multiplied (the 128 x 96 tiles are coarser
+ *                              than the sectors at bonds up to 256: no measured gain).
  * Used by the batched driver's autotuner (no reference counterpart). */
 enum {
   PTN_TUNE_TC_SPLIT_WAVES = 0,

@@ -24,7 +24,7 @@ void set_error(const char* fmt, ...) {
 void note_launches(int n) { g_launches.fetch_add((uint64_t)n, std::memory_order_relaxed); }
 
 namespace {
-std::atomic<int> g_tune[PTN_TUNE_COUNT] = {{1}, {2}, {0}, {0}, {1}, {0}, {1}, {0}};
+std::atomic<int> g_tune[PTN_TUNE_COUNT] = {{1}, {2}, {0}, {0}, {1}, {0}, {0}, {0}};
 constexpr int kTuneMax[PTN_TUNE_COUNT] = {16, 16, 5, 16, 1, 3, 1, 1};
 }  // namespace
 

@@ -264,6 +264,10 @@ __device__ __forceinline__ double finish_value(long long x, uint32_t a3, uint32_
 // operand tiles non-zero, as four 32-bit masks; all lanes of the warp take part
 __device__ __forceinline__ int unit_mask(const TcArgs& p, int m0, int n0, int k0, int k1, int lane,
                                          uint32_t (&mk)[4]) {
+  if (p.fa == nullptr) {   // dense: every block of the unit (uniform over the launch)
+    mk[0] = mk[1] = mk[2] = mk[3] = 0xffffffffu;
+    return k1 - k0;
+  }
   int n = 0;
 #pragma unroll
   for (int w = 0; w < 4; ++w) {
@@ -277,8 +281,11 @@ __device__ __forceinline__ int unit_mask(const TcArgs& p, int m0, int n0, int k0
   return n;
 }
 
+// bit j of the unit mask (selects, no dynamically indexed register array); always
+// set when the GEMM has no zero-tile flags
 __device__ __forceinline__ bool mask_bit(const uint32_t (&mk)[4], int j) {
-  return (mk[j >> 5] >> (j & 31)) & 1u;
+  const uint32_t w = (j < 64) ? ((j < 32) ? mk[0] : mk[1]) : ((j < 96) ? mk[2] : mk[3]);
+  return (w >> (j & 31)) & 1u;
 }
 
 // the MMAs of digit pairs [P0, P1) of one K block (stage addresses a0 / b0); the
@@ -1019,7 +1026,9 @@ ptn_status tc_gemm(const void* Aslices, long aplane, const int* ea, const void* 
   const int prof = prof_begin(st, PROF_TC_GEMM, 8.0 * M * (double)Nc * Kc,
                               2.0 * NDIGIT * ((double)M * Kp + (double)N * Kp) + 16.0 * M * Nc);
   const long units = (long)gx * gy * splits;
-  if (tune(PTN_TUNE_TC_PERSISTENT) != 0 && units <= INT_MAX) {
+  // the persistent form when asked for, and always for zero-tile skipping (only it
+  // reads the flags); one CTA per unit otherwise (measured faster on dense data)
+  if ((tune(PTN_TUNE_TC_PERSISTENT) != 0 || flags) && units <= INT_MAX) {
     const int grid = (int)std::min<long>(units, num_sms());
     tc_gemm_persistent_kernel<<<grid, THREADS, SMEM_BYTES, st>>>(ma, mb, a, gx, gy, (int)units);
   } else {

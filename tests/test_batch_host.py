@@ -48,7 +48,7 @@ def test_tuning_knobs_validate_and_round_trip():
     assert L.ptn_tune_set(_lib.TUNE_LARFB_TILE, 9) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_set(_lib.TUNE_QR_PANEL, 4) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, 2) == _lib.PTN_BAD_SHAPE
-    assert L.ptn_tune_get(_lib.TUNE_QR_PANEL) == 0 and L.ptn_tune_get(_lib.TUNE_TC_PERSISTENT) == 1
+    assert L.ptn_tune_get(_lib.TUNE_QR_PANEL) == 0 and L.ptn_tune_get(_lib.TUNE_TC_PERSISTENT) == 0
     assert L.ptn_tune_set(8, 1) == _lib.PTN_BAD_SHAPE
     assert L.ptn_tune_get(_lib.TUNE_TC_SKIP_ZERO) == 0
     assert L.ptn_tune_get(_lib.TUNE_TC_SPLIT_WAVES) == 1

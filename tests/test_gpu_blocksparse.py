@@ -103,8 +103,8 @@ def test_blocksparse_saves_time_at_larger_bonds():
 def test_digit_gemm_skips_zero_tiles_exactly():
     """Operands with quantum-number-like zero blocks: the digit GEMM with zero-tile
     skipping (PTN_TUNE_TC_SKIP_ZERO 1: the K blocks where the A or the B tile is
-    zero are not multiplied) gives the same bits as without it, and as the
-    one-CTA-per-unit kernel."""
+    zero are not multiplied) gives the same bits as the persistent and the
+    one-CTA-per-unit kernels without it."""
     import torch
     from pytenet_gb300 import _lib
     from pytenet_gb300.device import to_dev, to_host, ptr, stream_ptr, empty
@@ -121,7 +121,7 @@ def test_digit_gemm_skips_zero_tiles_exactly():
     out = {}
     old = (L.ptn_tune_get(_lib.TUNE_TC_PERSISTENT), L.ptn_tune_get(_lib.TUNE_TC_SKIP_ZERO))
     try:
-        for pers, skip in ((1, 1), (1, 0), (0, 1)):
+        for pers, skip in ((1, 1), (1, 0), (0, 0)):
             assert L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, pers) == 0
             assert L.ptn_tune_set(_lib.TUNE_TC_SKIP_ZERO, skip) == 0
             dA, dB, dC = to_dev(A), to_dev(B), empty((M, N))
@@ -135,7 +135,7 @@ def test_digit_gemm_skips_zero_tiles_exactly():
         L.ptn_tune_set(_lib.TUNE_TC_PERSISTENT, old[0])
         L.ptn_tune_set(_lib.TUNE_TC_SKIP_ZERO, old[1])
     assert np.array_equal(out[(1, 1)], out[(1, 0)])
-    assert np.array_equal(out[(1, 1)], out[(0, 1)])
+    assert np.array_equal(out[(1, 1)], out[(0, 0)])
     ref = A @ B
     assert np.linalg.norm(out[(1, 1)] - ref) < 1e-10 * np.linalg.norm(ref)
 
