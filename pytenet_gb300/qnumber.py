@@ -40,10 +40,12 @@ def is_qsparse(a, qnums):
     """Whether every entry with a non-zero quantum-number sum vanishes
     (pytenet/block_sparse_util.py:47-53). Accepts NumPy arrays or device tensors."""
     mask = qnumber_outer_sum(qnums) != 0
+    if not mask.any():
+        return True   # no entry is constrained (e.g. all quantum numbers zero)
     if hasattr(a, "is_cuda"):
         import torch
-        m = torch.from_numpy(np.array(np.broadcast_to(mask, tuple(a.shape)))).to(a.device)
-        return not bool(torch.any(a[m] != 0).item())
+        m = torch.from_numpy(np.ascontiguousarray(np.broadcast_to(mask, tuple(a.shape))))
+        return not bool(torch.any((a != 0) & m.to(a.device)).item())
     a = np.asarray(a)
     return not np.any(np.where(mask, a, 0))
 
