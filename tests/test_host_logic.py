@@ -164,3 +164,43 @@ def test_merge_mpo_pair_matches_oracle():
     w0 = rng.normal(size=(3, 2, 2, 4))
     w1 = rng.normal(size=(4, 2, 2, 5))
     assert np.allclose(merge_mpo_pair(w0, w1), orc._mpo_merge_pair(w0, w1), rtol=0, atol=1e-14)
+
+
+def test_density_compression_column_order_matches_block_sparse_eigh():
+    """compression._eigh_order puts the block SVD's columns (sorted quantum-number
+    blocks, values descending) into block_sparse_eigh's order (blocks in the
+    iteration order of the Python set of the row quantum numbers, eigenvalues
+    ascending; pytenet/block_sparse_util.py:183-241). Checked on a Hermitian
+    positive semidefinite block-sparse matrix with a NumPy SVD per plan block:
+    the permuted singular values equal the oracle's |eigenvalues| and the permuted
+    quantum numbers its bond quantum numbers, position by position."""
+    from pytenet_gb300.compression import _eigh_order
+    from pytenet_gb300.qnumber import qr_plan
+    rng = np.random.default_rng(7)
+    q = rng.choice([-3, -1, 0, 1, 2, 5], size=40)
+    b = orc.crandn((40, 40), rng)
+    b[q[:, None] != q[None, :]] = 0
+    rho = b @ b.conj().T                       # block-diagonal in q, PSD
+    plan = qr_plan(q, q)
+    s = np.zeros(plan.K)
+    for rows, cols, k0, kb in plan.blocks:
+        s[k0:k0 + kb] = np.linalg.svd(rho[np.ix_(rows, cols)], compute_uv=False)
+    perm = _eigh_order(plan, q)
+    u, ev, qe = orc.block_sparse_eigh(rho, q)
+    assert sorted(perm.tolist()) == list(range(plan.K))
+    assert np.array_equal(plan.qinterm[perm], qe)
+    assert np.allclose(s[perm], np.abs(ev), rtol=0, atol=1e-10 * np.abs(ev).max())
+
+
+def test_is_qsparse_without_constraints_and_with_violations():
+    """is_qsparse (pytenet/block_sparse_util.py:47-53): nothing is constrained when
+    every quantum-number sum is zero (any tensor passes, without looking at it);
+    with quantum numbers a non-zero entry at a non-zero sum is detected."""
+    from pytenet_gb300.qnumber import is_qsparse, enforce_qsparsity
+    rng = np.random.default_rng(8)
+    a = orc.crandn((4, 2, 5), rng)
+    assert is_qsparse(a, [np.zeros(4, int), np.zeros(2, int), np.zeros(5, int)])
+    qn = [np.array([0, 1, -1, 2]), np.array([1, -1]), -np.array([1, 0, -1, 2, 3])]
+    assert not is_qsparse(a, qn) and not orc.is_qsparse(a, qn)
+    enforce_qsparsity(a, qn)
+    assert is_qsparse(a, qn) and orc.is_qsparse(a, qn)
