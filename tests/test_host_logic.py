@@ -83,6 +83,8 @@ def test_hamiltonians_equal_reference_operators(L):
     import pytenet_gb300 as ptg
     g = load_golden("mpos.npz")
     h = ptg.heisenberg_xxz_1d_mpo(L, 1.3, 0.7, -0.2)
+    # the reference's bond dimensions: 4 next to the chain ends, 5 in the bulk
+    assert list(h.bond_dims) == [1] + [4] + [5] * (L - 3) + [4] * (L > 2) + [1]
     assert np.allclose(h.to_matrix(), g[f"xxz{L}_mat"], rtol=0, atol=1e-14)
     assert np.allclose(orc.mpo_to_matrix(h), g[f"xxz{L}_mat"], rtol=0, atol=1e-14)
     for i, w in enumerate(h.a):
